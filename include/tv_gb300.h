@@ -1,0 +1,107 @@
+/*
+ * tv_gb300.h -- C ABI of the GB300 HSMM tensor-Viterbi decoder.
+ *
+ * Plain pointers and sizes only.  Every array is row-major and float64 unless
+ * stated otherwise, in the Python-facing layouts of the reference binding
+ * (src/bindings.cpp:19-32):
+ *   trans_mat             (N, N) log space, indexed [to j][from i]
+ *   emission_probs        (O, N) log space
+ *   duration_probs_linear (D, N) linear space (accepted, not read: the
+ *                         decoder follows the reference C++ backend, whose
+ *                         tail uses the log-space survival function)
+ *   start_probs           (N,)   log space
+ *   duration_probs        (D, N) log space
+ *   obs_seq               (T,)   0-based symbols, int32
+ * The decoded path is int32 (T,).  The path log-likelihood is the
+ * tail-adjusted score of the best final state, the value the reference's
+ * backtrace starts from (src/hsmm.cu:147-155).
+ *
+ * Errors are returned as TV_* status codes; the library never exits the
+ * process.  tv_last_error() gives a message for the calling thread.
+ */
+#ifndef TV_GB300_H
+#define TV_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum tv_status {
+    TV_OK = 0,
+    TV_EINVAL = -1,     /* bad argument: size, null pointer, shape */
+    TV_ESHORT = -2,     /* T < D: the reference initialisation reads obs[0..D) */
+    TV_ERANGE = -3,     /* an observation outside [0, O) */
+    TV_ENONFINITE = -4, /* NaN or +-inf in a model table */
+    TV_ETOOBIG = -5,    /* N or D above 65536, or T above 2^31-1 */
+    TV_ENOMEM = -6,     /* device or host allocation failed */
+    TV_ECUDA = -7,      /* CUDA runtime error (see tv_last_error) */
+    TV_EINTERNAL = -8,  /* device-side consistency check failed */
+    TV_ENODEV = -9      /* no CUDA device */
+};
+
+/* Message for the last non-OK status returned on this thread. */
+const char* tv_last_error(void);
+
+/*
+ * One-shot decode with host buffers: the drop-in for the reference's
+ * hsmm::decode_tensor_viterbi_cuda (src/hsmm.hpp:48-56, src/hsmm.cu:604-720)
+ * as bound by src/bindings.cpp:104-114 and called from
+ * tensor_viterbi/viterbi/native.py:67-81.  Same arguments; the caller owns
+ * path_out (T int32).  loglik_out may be NULL.  Synchronous; device 0.
+ */
+int tv_decode_tensor_viterbi_cuda(int n_states, int n_symbols, int max_dur, int64_t T,
+                                  const double* trans_mat, const double* emission_probs,
+                                  const double* duration_probs_linear, const double* start_probs,
+                                  const double* duration_probs, const int32_t* obs_seq,
+                                  int32_t* path_out, double* loglik_out);
+
+/*
+ * Device-resident model: the tables the reference uploads per call in
+ * hsmm_to_gpu (src/hsmm.cu:173-201), uploaded once and reused.  Host
+ * pointers in the layouts above.  tv_model_destroy frees it.
+ */
+typedef struct tv_model_s* tv_model;
+int tv_model_create(int n_states, int n_symbols, int max_dur,
+                    const double* trans_mat, const double* emission_probs,
+                    const double* duration_probs_linear, const double* start_probs,
+                    const double* duration_probs, tv_model* out);
+int tv_model_destroy(tv_model m);
+
+/* Decode one sequence with host buffers through a model (synchronous).
+ * Replaces the per-call body of src/hsmm.cu:604-720 after the upload. */
+int tv_decode(tv_model m, const int32_t* obs_seq, int64_t T,
+              int32_t* path_out, double* loglik_out);
+
+/* Decode one sequence whose observations are already in device memory.
+ * obs_dev (T int32), path_dev (T int32) and loglik_dev (1 double, may be
+ * NULL) are device pointers; the call is asynchronous on `stream`
+ * (a cudaStream_t, NULL = legacy default stream).  Scratch memory is owned
+ * by the model and reused; calls on one model must not overlap. */
+int tv_decode_device(tv_model m, const int32_t* obs_dev, int64_t T,
+                     int32_t* path_dev, double* loglik_dev, void* stream);
+
+/* Batched decode: n_seq independent sequences that share the model, in one
+ * persistent launch.  No reference counterpart (the reference decodes one
+ * sequence per call); each result equals the single-sequence decode.
+ * obs_cat holds the sequences back to back, offsets[k]..offsets[k+1]
+ * (n_seq+1 int64 entries) delimit sequence k, and path_cat has the same
+ * shape.  Host buffers, synchronous.  loglik_out (n_seq) may be NULL. */
+int tv_decode_batch(tv_model m, int n_seq, const int64_t* offsets,
+                    const int32_t* obs_cat, int32_t* path_cat, double* loglik_out);
+
+/* Device-pointer form of tv_decode_batch (asynchronous on `stream`);
+ * offsets stays a host array, obs_cat/path_cat/loglik_dev are device
+ * pointers. */
+int tv_decode_batch_device(tv_model m, int n_seq, const int64_t* offsets,
+                           const int32_t* obs_cat_dev, int32_t* path_cat_dev,
+                           double* loglik_dev, void* stream);
+
+/* Number of kernel launches the most recent decode on this model issued
+ * (diagnostics for benchmark reporting). */
+int64_t tv_model_last_launches(tv_model m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

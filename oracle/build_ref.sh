@@ -1,0 +1,50 @@
+#!/usr/bin/env bash
+# Compiles the reference project's own CPU decoders (its pybind11 module
+# `_native`, built from src/hsmm.cu + src/bindings.cpp with -DNO_GPU) straight
+# from the read-only reference checkout into oracle/_ref/.  Nothing is copied
+# into this repository: the sources are compiled where they lie.
+#
+# Two builds are produced:
+#   oracle/_ref/shipped/_native*.so  the reference's own CPU flags
+#                                    (CMakeLists.txt:131-136: -O3 -march=native
+#                                    -mtune=native -ffast-math, OpenMP)
+#   oracle/_ref/ieee/_native*.so     the same sources with plain IEEE
+#                                    arithmetic (-O2, OpenMP, no fast-math), the
+#                                    build the C restatement is pinned to
+#
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Exits 0 without building when the reference checkout or pybind11 is absent.
+set -euo pipefail
+REF="${1:-/root/reference}"
+HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+OUT="$HERE/_ref"
+if [[ ! -f "$REF/src/hsmm.cu" || ! -f "$REF/src/bindings.cpp" ]]; then
+    echo "build_ref: reference sources not found under $REF; skipping" >&2
+    exit 0
+fi
+PY="${PYTHON:-python3}"
+if ! PYBIND_INC="$($PY -c 'import pybind11; print(pybind11.get_include())' 2>/dev/null)"; then
+    echo "build_ref: pybind11 not importable; skipping" >&2
+    exit 0
+fi
+PY_INC="$($PY -c 'import sysconfig; print(sysconfig.get_path("include"))')"
+SUFFIX="$($PY -c 'import sysconfig; print(sysconfig.get_config_var("EXT_SUFFIX"))')"
+
+build() {
+    local name="$1"; shift
+    mkdir -p "$OUT/$name"
+    local obj="$OUT/$name/_native$SUFFIX"
+    if [[ -f "$obj" && "$obj" -nt "$REF/src/hsmm.cu" && "$obj" -nt "$REF/src/bindings.cpp" ]]; then
+        return 0
+    fi
+    g++ -std=c++17 -shared -fPIC -DNO_GPU "$@" -fopenmp \
+        -I"$REF/src" -isystem "$PY_INC" -isystem "$PYBIND_INC" \
+        -x c++ "$REF/src/hsmm.cu" -x c++ "$REF/src/bindings.cpp" \
+        -o "$obj.tmp"
+    mv "$obj.tmp" "$obj"
+    echo "build_ref: built $obj"
+}
+
+build shipped -O3 -march=native -mtune=native -ffast-math &
+build ieee -O2 &
+wait

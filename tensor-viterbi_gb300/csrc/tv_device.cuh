@@ -1,0 +1,91 @@
+// tv_device.cuh -- device-side building blocks shared by the decode kernels.
+//
+// Scores are compared in int64 fixed point (value * 2^f, f chosen per decode
+// on the host).  GB300 issues FP64 at 1/64 of the FP32 rate, so the per-cell
+// max-plus scan runs on the integer pipes; FP64 is kept for the values the
+// reference defines bit for bit (the emission window sums and the winners'
+// scores).  A candidate is only trusted when it beats every other one by more
+// than the certified margin; otherwise the candidates inside the margin are
+// re-scored exactly in FP64 with the reference's association and tie order.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tv {
+
+// Below every reachable fixed-point score (|score| < 2^61 by the choice of f),
+// and far enough from INT64_MIN that b1 - b2 never overflows.
+constexpr long long QNEG = -(1LL << 62);
+constexpr int IDX_NONE = 0x7fffffff;
+
+// Back-pointer word: (d << 16) | i, where d+1 is the segment length and i the
+// previous state.  N and D are limited to 65536.
+__device__ __forceinline__ uint32_t pack_psi(int d, int i) {
+  return ((uint32_t)d << 16) | (uint32_t)i;
+}
+
+// Running best / second best of a fixed-point scan with the index of the
+// best.  Inside one lane indices arrive in increasing order, so a strict '>'
+// keeps the lowest index of an exact tie.
+struct Top2 {
+  long long b1;
+  long long b2;
+  int x1;
+  __device__ __forceinline__ void init() { b1 = QNEG; b2 = QNEG; x1 = IDX_NONE; }
+  __device__ __forceinline__ void push(long long v, int x) {
+    const bool take = v > b1;
+    const long long lose = take ? b1 : v;
+    b2 = lose > b2 ? lose : b2;
+    if (take) { b1 = v; x1 = x; }
+  }
+  // Merge another lane's state; equal best values keep the lower index.
+  __device__ __forceinline__ void merge(long long ob1, int ox1, long long ob2) {
+    const bool take = (ob1 > b1) || (ob1 == b1 && ox1 < x1);
+    const long long lose = take ? b1 : ob1;
+    long long s = b2 > ob2 ? b2 : ob2;
+    s = s > lose ? s : lose;
+    if (take) { b1 = ob1; x1 = ox1; }
+    b2 = s;
+  }
+  // Butterfly reduction: every lane ends with the warp-wide result.
+  __device__ __forceinline__ void warp_reduce() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long ob1 = __shfl_xor_sync(0xffffffffu, b1, o);
+      const long long ob2 = __shfl_xor_sync(0xffffffffu, b2, o);
+      const int ox1 = __shfl_xor_sync(0xffffffffu, x1, o);
+      merge(ob1, ox1, ob2);
+    }
+  }
+};
+
+// Exact candidate in the reference's order: the larger value wins, then the
+// lower d, then the lower i (the d-outer / i-inner strict '>' scan of
+// src/hsmm.cu:340-350).
+struct ExactBest {
+  double v;
+  int d;
+  int i;
+  __device__ __forceinline__ void init() { v = -__longlong_as_double(0x7ff0000000000000LL); d = IDX_NONE; i = IDX_NONE; }
+  __device__ __forceinline__ bool better(double ov, int od, int oi) const {
+    return (ov > v) || (ov == v && (od < d || (od == d && oi < i)));
+  }
+  __device__ __forceinline__ void offer(double ov, int od, int oi) {
+    if (better(ov, od, oi)) { v = ov; d = od; i = oi; }
+  }
+  __device__ __forceinline__ void warp_reduce() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ov = __shfl_xor_sync(0xffffffffu, v, o);
+      const int od = __shfl_xor_sync(0xffffffffu, d, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, i, o);
+      offer(ov, od, oi);
+    }
+  }
+};
+
+__device__ __forceinline__ long long quantize(double x, double scale) {
+  return __double2ll_rn(x * scale);
+}
+
+}  // namespace tv

@@ -1,0 +1,198 @@
+"""Drop-in replacement for the reference's `tensor_viterbi/viterbi/native.py`
+CUDA backend (native.py:67-81 there), backed by the GB300 decoder.
+
+`decode_tensor_viterbi_cuda(n_states, trans_mat, emission_probs,
+duration_probs_linear, start_probs, duration_probs, obs_seq)` keeps the
+reference signature, argument meaning and layouts (src/bindings.cpp:19-32):
+log-space (N,N) transitions indexed [to j][from i], (O,N) emissions, (D,N)
+linear and log duration pmfs, (N,) start, 0-based observations (any numeric
+dtype, cast like the binding's forcecast).  It returns a fresh int32 (T,)
+path that equals the reference C++ backend's path.
+
+`configure(system, toolchain)` is kept for callers such as the reference
+benchmark app: the arguments are accepted and ignored, and it loads the GB300
+library.  As in the reference, decoding before `configure` raises
+RuntimeError.  The C++ and OpenMP CPU backends are not part of this build;
+their entry points raise RuntimeError like an absent backend does in the
+reference (native.py:77-79).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+
+_native = None
+_sys_name: str = ""
+
+
+def configure(system: str = "", toolchain: str = "") -> None:
+    """Load the GB300 decoder library.  `system`/`toolchain` are accepted for
+    compatibility with the reference's per-system builds and ignored."""
+    global _native, _sys_name
+    _sys_name = f"{system}/{toolchain}"
+    try:
+        _native = _lib.lib()
+    except OSError as e:  # pragma: no cover - loader failure
+        raise RuntimeError(f"[native] Could not load the GB300 decoder library: {e}") from e
+
+
+def _ensure_configured() -> None:
+    if _native is None:
+        raise RuntimeError(
+            "[native] Native extension not loaded.\n"
+            "Call tensor_viterbi.viterbi.native.configure(system, toolchain) first."
+        )
+
+
+def _f64(x) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+
+
+def _obs_i32(x) -> np.ndarray:
+    a = np.asarray(x)
+    if a.dtype != np.int32:
+        a = a.astype(np.int32)
+    return np.ascontiguousarray(a.reshape(-1))
+
+
+def _model_arrays(n_states, trans_mat, emission_probs, duration_probs_linear, start_probs, duration_probs):
+    N = int(n_states)
+    tm = _f64(trans_mat)
+    ep = _f64(emission_probs)
+    dl = _f64(duration_probs_linear)
+    sp = _f64(start_probs).reshape(-1)
+    dp = _f64(duration_probs)
+    if ep.ndim != 2 or dp.ndim != 2:
+        raise ValueError("[native] emission_probs and duration_probs must be 2-D")
+    O, D = ep.shape[0], dp.shape[0]
+    if tm.shape != (N, N):
+        raise ValueError(f"[native] trans_mat has shape {tm.shape}, expected ({N}, {N})")
+    if ep.shape != (O, N):
+        raise ValueError(f"[native] emission_probs has shape {ep.shape}, expected (O, {N})")
+    if dp.shape != (D, N):
+        raise ValueError(f"[native] duration_probs has shape {dp.shape}, expected (D, {N})")
+    if dl.shape != (D, N):
+        raise ValueError(f"[native] duration_probs_linear has shape {dl.shape}, expected ({D}, {N})")
+    if sp.shape != (N,):
+        raise ValueError(f"[native] start_probs has shape {sp.shape}, expected ({N},)")
+    return N, O, D, tm, ep, dl, sp, dp
+
+
+class Model:
+    """A device-resident HSMM (the tables the reference uploads on every call,
+    src/hsmm.cu:173-201, uploaded once).  Reuse it to decode many sequences."""
+
+    def __init__(self, n_states, trans_mat, emission_probs, duration_probs_linear, start_probs, duration_probs):
+        L = _lib.lib()
+        N, O, D, tm, ep, dl, sp, dp = _model_arrays(
+            n_states, trans_mat, emission_probs, duration_probs_linear, start_probs, duration_probs)
+        self.N, self.O, self.D = N, O, D
+        h = C.c_void_p()
+        _lib.check(L.tv_model_create(N, O, D, _lib.dptr(tm), _lib.dptr(ep), _lib.dptr(dl),
+                                     _lib.dptr(sp), _lib.dptr(dp), C.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.lib().tv_model_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def decode(self, obs_seq, return_loglik: bool = False):
+        """Decode one sequence (host arrays in and out, synchronous)."""
+        obs = _obs_i32(obs_seq)
+        T = obs.size
+        path = np.empty(T, dtype=np.int32)
+        ll = np.zeros(1, dtype=np.float64)
+        _lib.check(_lib.lib().tv_decode(self._h, _lib.iptr(obs), T, _lib.iptr(path), _lib.dptr(ll)))
+        return (path, float(ll[0])) if return_loglik else path
+
+    def decode_batch(self, sequences, return_loglik: bool = False):
+        """Decode many sequences of any lengths in one persistent launch."""
+        seqs = [_obs_i32(s) for s in sequences]
+        off = np.zeros(len(seqs) + 1, dtype=np.int64)
+        off[1:] = np.cumsum([s.size for s in seqs])
+        cat = np.ascontiguousarray(np.concatenate(seqs)) if seqs else np.zeros(0, np.int32)
+        out = np.empty(int(off[-1]), dtype=np.int32)
+        ll = np.zeros(len(seqs), dtype=np.float64)
+        _lib.check(_lib.lib().tv_decode_batch(self._h, len(seqs), _lib.lptr(off), _lib.iptr(cat),
+                                              _lib.iptr(out), _lib.dptr(ll)))
+        paths = [out[off[k]:off[k + 1]] for k in range(len(seqs))]
+        return (paths, ll) if return_loglik else paths
+
+    def decode_device(self, obs_dev_ptr: int, T: int, path_dev_ptr: int, loglik_dev_ptr: int = 0,
+                      stream: int = 0) -> None:
+        """Asynchronous decode of device-resident observations (raw device
+        pointers, e.g. torch `data_ptr()`), on `stream` (a cudaStream_t)."""
+        _lib.check(_lib.lib().tv_decode_device(self._h, C.c_void_p(obs_dev_ptr), int(T),
+                                               C.c_void_p(path_dev_ptr), C.c_void_p(loglik_dev_ptr or None),
+                                               C.c_void_p(stream or None)))
+
+    def decode_batch_device(self, offsets: np.ndarray, obs_dev_ptr: int, path_dev_ptr: int,
+                            loglik_dev_ptr: int = 0, stream: int = 0) -> None:
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        _lib.check(_lib.lib().tv_decode_batch_device(self._h, off.size - 1, _lib.lptr(off),
+                                                     C.c_void_p(obs_dev_ptr), C.c_void_p(path_dev_ptr),
+                                                     C.c_void_p(loglik_dev_ptr or None),
+                                                     C.c_void_p(stream or None)))
+
+    def last_launches(self) -> int:
+        return int(_lib.lib().tv_model_last_launches(self._h))
+
+
+def decode_tensor_viterbi_cuda_loglik(n_states, trans_mat, emission_probs, duration_probs_linear,
+                                      start_probs, duration_probs, obs_seq):
+    """Like decode_tensor_viterbi_cuda, also returning the path log-likelihood."""
+    _ensure_configured()
+    N, O, D, tm, ep, dl, sp, dp = _model_arrays(
+        n_states, trans_mat, emission_probs, duration_probs_linear, start_probs, duration_probs)
+    obs = _obs_i32(obs_seq)
+    path = np.empty(obs.size, dtype=np.int32)
+    ll = np.zeros(1, dtype=np.float64)
+    _lib.check(_native.tv_decode_tensor_viterbi_cuda(
+        N, O, D, obs.size, _lib.dptr(tm), _lib.dptr(ep), _lib.dptr(dl), _lib.dptr(sp), _lib.dptr(dp),
+        _lib.iptr(obs), _lib.iptr(path), _lib.dptr(ll)))
+    return path, float(ll[0])
+
+
+def decode_tensor_viterbi_cuda(
+        n_states,
+        trans_mat,
+        emission_probs,
+        duration_probs_linear,
+        start_probs,
+        duration_probs,
+        obs_seq,
+) -> np.ndarray:
+    return decode_tensor_viterbi_cuda_loglik(n_states, trans_mat, emission_probs, duration_probs_linear,
+                                             start_probs, duration_probs, obs_seq)[0]
+
+
+def decode_tensor_viterbi_cpp(n_states, trans_mat, emission_probs, duration_probs_linear, start_probs,
+                              duration_probs, obs_seq) -> np.ndarray:
+    _ensure_configured()
+    raise RuntimeError("C++ backend not available in this build.")
+
+
+def decode_tensor_viterbi_omp(n_states, trans_mat, emission_probs, duration_probs_linear, start_probs,
+                              duration_probs, obs_seq) -> np.ndarray:
+    _ensure_configured()
+    raise RuntimeError("OMP backend not available in this build.")

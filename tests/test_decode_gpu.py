@@ -1,0 +1,80 @@
+"""GPU parity: the CUDA decoder, called through the C ABI, against the
+reference's golden paths and the CPU oracle.
+
+Bar: paths bit-exact; the log-likelihood bit-exact against the oracle's
+(both follow the reference association) and within 1e-9 relative of the
+independent long-double segment scorer.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+LL_RTOL = 1e-9
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_golden_paths(tvlib, name):
+    args, z = load_golden(name)
+    path, ll = tvlib.decode_tensor_viterbi_cuda_loglik(*args)
+    np.testing.assert_array_equal(path, z["path_cpp"])
+    ref = orc.decode(*args, tables=True)
+    assert ll == ref["loglik"], (ll, ref["loglik"])
+    if np.isfinite(ll):
+        N, tm, em, _, sp, dp, obs = args
+        sc = orc.score_segments(N, tm, em, sp, dp, obs, ref["path"], ref["seg_start"])
+        assert abs(ll - sc) <= LL_RTOL * abs(sc)
+
+
+def test_dropin_signature_returns_int32_path(tvlib):
+    args, z = load_golden("syn_config0")
+    out = tvlib.decode_tensor_viterbi_cuda(*args)
+    assert out.dtype == np.int32 and out.shape == z["path_cpp"].shape
+    np.testing.assert_array_equal(out, z["path_cpp"])
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_models_vs_oracle(tvlib, seed):
+    import tensor_viterbi.synthetic as syn
+    rng = np.random.default_rng(1000 + seed)
+    N = int(rng.integers(1, 40))
+    D = int(rng.integers(1, 120))
+    T = int(rng.integers(D, D + 1500))
+    M = int(rng.integers(2, 20))
+    lo = float(rng.uniform(1, max(2, D / 2)))
+    hi = float(rng.uniform(lo, max(lo + 1, D)))
+    p = syn.discrete_problem(N, D, T, M, lo, hi, seed=seed)
+    ref = orc.decode(*p.args())
+    path, ll = tvlib.decode_tensor_viterbi_cuda_loglik(*p.args())
+    np.testing.assert_array_equal(path, ref["path"])
+    assert ll == ref["loglik"]
+
+
+def test_model_reuse_and_batch_equal_single(tvlib):
+    import tensor_viterbi.synthetic as syn
+    prob, seqs = syn.batch_problem(n_seq=24, N=10, D=60, M=16, lo=60, hi=3000, seed=5)
+    with tvlib.Model(*prob.model_args()) as m:
+        singles = [m.decode(s, return_loglik=True) for s in seqs]
+        paths, lls = m.decode_batch(seqs, return_loglik=True)
+    for (p1, l1), p2, l2, s in zip(singles, paths, lls, seqs):
+        np.testing.assert_array_equal(p1, p2)
+        assert l1 == l2
+        ref = orc.decode(*prob.model_args(), s)
+        np.testing.assert_array_equal(p1, ref["path"])
+        assert l1 == ref["loglik"]
+
+
+def test_errors_are_returned_not_fatal(tvlib):
+    args, _ = load_golden("syn_config0")
+    N, tm, em, dl, sp, dp, obs = args
+    with pytest.raises(ValueError, match="T="):
+        tvlib.decode_tensor_viterbi_cuda(N, tm, em, dl, sp, dp, obs[:10])
+    bad = obs.copy()
+    bad[3] = 99
+    with pytest.raises(ValueError, match="outside"):
+        tvlib.decode_tensor_viterbi_cuda(N, tm, em, dl, sp, dp, bad)
+    # the library stays usable after an error
+    np.testing.assert_array_equal(tvlib.decode_tensor_viterbi_cuda(*args), orc.decode(*args)["path"])
