@@ -37,7 +37,8 @@ enum tv_status {
     TV_ENOMEM = -6,     /* device or host allocation failed */
     TV_ECUDA = -7,      /* CUDA runtime error (see tv_last_error) */
     TV_EINTERNAL = -8,  /* device-side consistency check failed */
-    TV_ENODEV = -9      /* no CUDA device */
+    TV_ENODEV = -9,     /* no CUDA device */
+    TV_ETIMEOUT = -10   /* a bounded device-side wait gave up (no progress) */
 };
 
 /* Message for the last non-OK status returned on this thread. */
@@ -100,6 +101,19 @@ int tv_decode_batch_device(tv_model m, int n_seq, const int64_t* offsets,
 /* Number of kernel launches the most recent decode on this model issued
  * (diagnostics for benchmark reporting). */
 int64_t tv_model_last_launches(tv_model m);
+
+/* Kernel selection for single-sequence decodes (no reference counterpart):
+ * TV_PATH_AUTO picks the one-CTA kernel when the D-deep window fits one
+ * CTA's shared memory and the whole-GPU grid kernel otherwise;
+ * TV_PATH_CTA / TV_PATH_GRID force one of them.  grid_ctas > 0 caps the
+ * grid kernel's CTA count (0 = one per SM).  Both kernels give identical
+ * results. */
+enum tv_path { TV_PATH_AUTO = 0, TV_PATH_CTA = 1, TV_PATH_GRID = 2 };
+int tv_model_set_path(tv_model m, int path, int grid_ctas);
+
+/* Which kernel the most recent single-sequence decode used (TV_PATH_CTA or
+ * TV_PATH_GRID). */
+int tv_model_last_path(tv_model m);
 
 #ifdef __cplusplus
 }

@@ -21,6 +21,7 @@
 
 #include "../../include/tv_gb300.h"
 #include "tv_cta.cuh"
+#include "tv_grid.cuh"
 
 namespace {
 
@@ -115,6 +116,15 @@ struct tv_model_s {
   DevBuf<double> ll_tmp;
   int64_t last_launches = 0;
   int sm_count = 0;
+  // grid-kernel scratch (single long sequences)
+  DevBuf<long long> slot_ctil;
+  DevBuf<unsigned short> slot_itil;
+  DevBuf<double> slot_dsel, dstar_g, dinit, ck;
+  DevBuf<unsigned long long> part;
+  DevBuf<int> seg_first, seg_count, seg_base, gflags;
+  int plan_key_N = -1, plan_key_D = -1, plan_key_G = -1;
+  tv::GridParams plan{};
+  int path_pref = TV_PATH_AUTO, grid_ctas = 0, last_path = 0;
   std::mutex mu;
 };
 
@@ -248,6 +258,188 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
   return TV_OK;
 }
 
+
+// Splits the N*D window cells (state-major, ring slot minor) into equal
+// contiguous chunks, one per worker CTA; a chunk's intersection with a
+// state's row is a segment and yields one partial winner per step.
+bool plan_grid(tv_model_s* m, int G, int smem_optin, tv::GridParams& P, std::vector<int>& first,
+               std::vector<int>& count, std::vector<int>& base) {
+  const int N = m->N, D = m->D, L = tv::GRID_L;
+  if (G < 2 || D <= L || N > tv::GRID_MAX_N || D > 65535) return false;
+  const int Gw = G - 1;
+  const long long ND = (long long)N * D;
+  const long long chunk = (ND + Gw - 1) / Gw;
+  first.assign(N, 0);
+  count.assign(N, 0);
+  base.assign(Gw, 0);
+  std::vector<int> seen(N, 0);
+  int S = 0, max_seg = 0;
+  for (int w = 0; w < Gw; ++w) {
+    const long long lo = (long long)w * chunk, hi = std::min(lo + chunk, ND);
+    base[w] = S;
+    if (lo >= hi) continue;
+    const int ja = (int)(lo / D), jb = (int)((hi - 1) / D);
+    for (int j = ja; j <= jb; ++j) {
+      if (!seen[j]) { seen[j] = 1; first[j] = S; }
+      count[j]++;
+      S++;
+    }
+    max_seg = std::max(max_seg, jb - ja + 1);
+  }
+  if (S > tv::GRID_THREADS || max_seg > 32) return false;
+  P = tv::GridParams{};
+  P.G = G; P.L = L; P.S = S; P.Rd = D + 2 * L + 8;
+  P.M = (D + tv::CK_STRIDE - 1) / tv::CK_STRIDE;
+  P.chunk = chunk; P.max_seg = max_seg;
+  unsigned long long o = 0;
+  P.w_qd = o;   o = tv::tv_align(o + (unsigned long long)max_seg * D * 8);
+  P.w_ctil = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
+  P.w_dsel = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
+  P.w_acc = o;  o = tv::tv_align(o + (unsigned long long)chunk * 8);
+  P.w_itil = o; o = tv::tv_align(o + (unsigned long long)chunk * 2);
+  P.w_red = o;  o = tv::tv_align(o + (unsigned long long)std::max(max_seg * 32 * sizeof(tv::Top2), 32 * sizeof(tv::ExactBest)));
+  P.w_bytes = o;
+  o = 0;
+  P.h_qtr = o;   o = tv::tv_align(o + (unsigned long long)N * N * 8);
+  P.h_ctil = o;  o = tv::tv_align(o + (unsigned long long)L * N * 8);
+  P.h_itil = o;  o = tv::tv_align(o + (unsigned long long)L * N * 2);
+  P.h_dstar = o; o = tv::tv_align(o + (unsigned long long)(L + 1) * N * 8);
+  P.h_E = o;     o = tv::tv_align(o + (unsigned long long)L * N * 8);
+  P.h_qd = o;    o = tv::tv_align(o + (unsigned long long)N * L * 8);
+  P.h_dur = o;   o = tv::tv_align(o + (unsigned long long)N * L * 8);
+  P.h_dq = o;    o = tv::tv_align(o + (unsigned long long)N * 8);
+  P.h_ptil = o;  o = tv::tv_align(o + (unsigned long long)N * 8);
+  P.h_pv = o;    o = tv::tv_align(o + (unsigned long long)S * 8);
+  P.h_pd = o;    o = tv::tv_align(o + (unsigned long long)S * 4);
+  P.h_pi = o;    o = tv::tv_align(o + (unsigned long long)S * 4);
+  P.h_tail = o;  o = tv::tv_align(o + (unsigned long long)N * 8);
+  P.h_red = o;
+  P.h_bytes = o;
+  P.timeout = 1LL << 31;  // SM clock cycles, about a second: no legitimate wait comes close
+  return std::max(P.w_bytes, P.h_bytes) + 256 <= (unsigned long long)smem_optin;
+}
+
+int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_dev, double* ll_dev,
+                cudaStream_t st, const tv::GridParams& P) {
+  const int N = m->N, D = m->D;
+  const Quant Q = choose_quant(m, T);
+  int rc;
+  if ((rc = prepare_quant(m, Q, st)) != TV_OK) return rc;
+  if ((rc = m->psi.ensure((size_t)T * N)) != TV_OK) return rc;
+  if ((rc = m->slot_ctil.ensure((size_t)tv::SLOT_RING * N)) != TV_OK) return rc;
+  if ((rc = m->slot_itil.ensure((size_t)tv::SLOT_RING * N)) != TV_OK) return rc;
+  if ((rc = m->slot_dsel.ensure((size_t)tv::SLOT_RING * N)) != TV_OK) return rc;
+  if ((rc = m->part.ensure((size_t)tv::PART_RING * P.S * 3)) != TV_OK) return rc;
+  if ((rc = m->dstar_g.ensure((size_t)P.Rd * N)) != TV_OK) return rc;
+  if ((rc = m->dinit.ensure((size_t)D * N)) != TV_OK) return rc;
+  const int tmax = (int)std::min<int64_t>(D, T - 1);
+  if ((rc = m->ck.ensure((size_t)std::max(tmax, 1) * P.M * N)) != TV_OK) return rc;
+  if ((rc = m->gflags.ensure(4)) != TV_OK) return rc;
+  TV_CUDA(cudaMemsetAsync(m->part.p, 0, sizeof(unsigned long long) * tv::PART_RING * P.S * 3, st));
+  TV_CUDA(cudaMemsetAsync(m->gflags.p, 0, sizeof(int) * 4, st));
+  tv::ModelView mv = view(m, Q);
+  int* gabort = m->gflags.p + 1;
+  int* gstatus = m->gflags.p + 2;
+  tv::grid_check_obs<<<64, 256, 0, st>>>(obs_dev, T, m->O, gabort, gstatus);
+  tv::grid_prep_init<<<(N + 127) / 128, 128, 0, st>>>(mv, obs_dev, m->dinit.p, gabort);
+  m->last_launches += 2;
+  if (tmax >= 1) {
+    const long long nthr = (long long)tmax * N;
+    tv::grid_prep_ck<<<(unsigned)((nthr + 255) / 256), 256, 0, st>>>(mv, obs_dev, m->ck.p, P.M, tmax, gabort);
+    m->last_launches += 1;
+  }
+  TV_CUDA(cudaGetLastError());
+  tv::GridBufs B;
+  B.obs = obs_dev;
+  B.T = T;
+  B.psi = m->psi.p;
+  B.path = path_dev;
+  B.loglik = ll_dev;
+  B.slot_ctil = m->slot_ctil.p;
+  B.slot_itil = m->slot_itil.p;
+  B.slot_dsel = m->slot_dsel.p;
+  B.part = m->part.p;
+  B.dstar_g = m->dstar_g.p;
+  B.dinit = m->dinit.p;
+  B.ck = m->ck.p;
+  B.seg_first = m->seg_first.p;
+  B.seg_count = m->seg_count.p;
+  B.seg_base = m->seg_base.p;
+  B.pub = (unsigned*)(m->gflags.p + 0);
+  B.abort_flag = m->gflags.p + 1;
+  B.status = m->gflags.p + 2;
+  tv::GridParams Pc = P;
+  void* args[] = {&mv, &Pc, &B};
+  const size_t dyn = std::max(P.w_bytes, P.h_bytes);
+  TV_CUDA(cudaFuncSetAttribute(tv::grid_decode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  TV_CUDA(cudaLaunchCooperativeKernel((void*)tv::grid_decode_kernel, dim3(P.G), dim3(tv::GRID_THREADS), args, dyn, st));
+  m->last_launches += 1;
+  return TV_OK;
+}
+
+// Picks and launches the kernel for one sequence on the device.
+int launch_single(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_dev, double* ll_dev,
+                  cudaStream_t st) {
+  if (T < m->D)
+    return fail(TV_ESHORT, "T=" + std::to_string(T) + " < D=" + std::to_string(m->D) +
+                               "; the reference initialisation needs T >= D");
+  int dev = 0;
+  TV_CUDA(cudaGetDevice(&dev));
+  int smem_optin = 0;
+  TV_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const tv::CtaLayout L = tv::make_cta_layout(m->N, m->D);
+  const bool cta_fits = L.bytes + 64 <= (size_t)smem_optin;
+  int want = m->path_pref;
+  if (want == TV_PATH_AUTO) want = cta_fits ? TV_PATH_CTA : TV_PATH_GRID;
+  if (want == TV_PATH_GRID) {
+    int per_sm = 0;
+    int G = m->sm_count;
+    if (m->grid_ctas > 0) G = std::min(G, m->grid_ctas);
+    if (m->plan_key_N != m->N || m->plan_key_D != m->D || m->plan_key_G != G) {
+      std::vector<int> first, count, base;
+      tv::GridParams P;
+      if (!plan_grid(m, G, smem_optin, P, first, count, base)) {
+        if (m->path_pref == TV_PATH_GRID)
+          return fail(TV_EINVAL, "the grid kernel cannot take this shape (needs D > 4, N <= 128, D <= 65535)");
+        want = TV_PATH_CTA;
+      } else {
+        const size_t dyn = std::max(P.w_bytes, P.h_bytes);
+        TV_CUDA(cudaFuncSetAttribute(tv::grid_decode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+        TV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tv::grid_decode_kernel, tv::GRID_THREADS, dyn));
+        if (per_sm < 1) return fail(TV_EINVAL, "grid kernel does not fit on an SM");
+        int rc;
+        if ((rc = m->seg_first.ensure(first.size())) != TV_OK) return rc;
+        if ((rc = m->seg_count.ensure(count.size())) != TV_OK) return rc;
+        if ((rc = m->seg_base.ensure(base.size())) != TV_OK) return rc;
+        TV_CUDA(cudaMemcpy(m->seg_first.p, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice));
+        TV_CUDA(cudaMemcpy(m->seg_count.p, count.data(), sizeof(int) * count.size(), cudaMemcpyHostToDevice));
+        TV_CUDA(cudaMemcpy(m->seg_base.p, base.data(), sizeof(int) * base.size(), cudaMemcpyHostToDevice));
+        m->plan = P;
+        m->plan_key_N = m->N;
+        m->plan_key_D = m->D;
+        m->plan_key_G = G;
+      }
+    }
+    if (want == TV_PATH_GRID) {
+      m->last_path = TV_PATH_GRID;
+      return launch_grid(m, obs_dev, T, path_dev, ll_dev, st, m->plan);
+    }
+  }
+  m->last_path = TV_PATH_CTA;
+  const int64_t off[2] = {0, T};
+  return launch_batch(m, 1, off, obs_dev, path_dev, ll_dev, st);
+}
+
+int read_grid_status(tv_model_s* m, cudaStream_t st) {
+  int s[4] = {0, 0, 0, 0};
+  TV_CUDA(cudaMemcpyAsync(s, m->gflags.p, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
+  TV_CUDA(cudaStreamSynchronize(st));
+  if (s[2] == tv::TV_ETIMEOUT_DEV) return fail(TV_ETIMEOUT, "grid decode: a bounded wait between CTAs timed out");
+  if (s[2] == TV_ERANGE) return fail(TV_ERANGE, "an observation is outside [0, O)");
+  if (s[2] != 0) return fail(TV_EINTERNAL, "grid decode: device back-pointer check failed");
+  return TV_OK;
+}
+
 int read_status(tv_model_s* m, int n_seq, cudaStream_t st) {
   std::vector<int> s((size_t)n_seq);
   TV_CUDA(cudaMemcpyAsync(s.data(), m->status.p, sizeof(int) * n_seq, cudaMemcpyDeviceToHost, st));
@@ -318,6 +510,9 @@ int tv_model_destroy(tv_model m) {
   m->em.release(); m->trans.release(); m->start.release(); m->durT.release(); m->survT.release();
   m->qem.release(); m->qtr.release(); m->qdurT.release();
   m->psi.release(); m->status.release(); m->counter.release(); m->off.release(); m->scratch.release();
+  m->slot_ctil.release(); m->slot_itil.release(); m->slot_dsel.release(); m->dstar_g.release();
+  m->dinit.release(); m->ck.release(); m->part.release();
+  m->seg_first.release(); m->seg_count.release(); m->seg_base.release(); m->gflags.release();
   m->obs_tmp.release(); m->path_tmp.release(); m->ll_tmp.release();
   delete m;
   return TV_OK;
@@ -325,14 +520,23 @@ int tv_model_destroy(tv_model m) {
 
 int64_t tv_model_last_launches(tv_model m) { return m ? m->last_launches : 0; }
 
+int tv_model_set_path(tv_model m, int path, int grid_ctas) {
+  if (!m || path < TV_PATH_AUTO || path > TV_PATH_GRID || grid_ctas < 0) return fail(TV_EINVAL, "bad path option");
+  std::lock_guard<std::mutex> lk(m->mu);
+  m->path_pref = path;
+  m->grid_ctas = grid_ctas;
+  return TV_OK;
+}
+
+int tv_model_last_path(tv_model m) { return m ? m->last_path : 0; }
+
 int tv_decode_device(tv_model m, const int32_t* obs_dev, int64_t T, int32_t* path_dev, double* ll_dev,
                      void* stream) {
   if (!m || !obs_dev || !path_dev) return fail(TV_EINVAL, "null argument");
   if (T <= 0 || T > 0x7fffffffLL) return fail(TV_ETOOBIG, "T must be in [1, 2^31-1]");
   std::lock_guard<std::mutex> lk(m->mu);
   m->last_launches = 0;
-  const int64_t off[2] = {0, T};
-  return launch_batch(m, 1, off, obs_dev, path_dev, ll_dev, (cudaStream_t)stream);
+  return launch_single(m, obs_dev, T, path_dev, ll_dev, (cudaStream_t)stream);
 }
 
 int tv_decode(tv_model m, const int32_t* obs, int64_t T, int32_t* path_out, double* loglik_out) {
@@ -347,12 +551,12 @@ int tv_decode(tv_model m, const int32_t* obs, int64_t T, int32_t* path_out, doub
   if ((rc = m->path_tmp.ensure((size_t)T)) != TV_OK) return rc;
   if ((rc = m->ll_tmp.ensure(1)) != TV_OK) return rc;
   TV_CUDA(cudaMemcpyAsync(m->obs_tmp.p, obs, sizeof(int32_t) * T, cudaMemcpyHostToDevice, st));
-  const int64_t off[2] = {0, T};
-  if ((rc = launch_batch(m, 1, off, m->obs_tmp.p, m->path_tmp.p, m->ll_tmp.p, st)) != TV_OK) return rc;
+  if ((rc = launch_single(m, m->obs_tmp.p, T, m->path_tmp.p, m->ll_tmp.p, st)) != TV_OK) return rc;
   TV_CUDA(cudaMemcpyAsync(path_out, m->path_tmp.p, sizeof(int32_t) * T, cudaMemcpyDeviceToHost, st));
   double ll = 0;
   TV_CUDA(cudaMemcpyAsync(&ll, m->ll_tmp.p, sizeof(double), cudaMemcpyDeviceToHost, st));
-  if ((rc = read_status(m, 1, st)) != TV_OK) return rc;
+  rc = (m->last_path == TV_PATH_GRID) ? read_grid_status(m, st) : read_status(m, 1, st);
+  if (rc != TV_OK) return rc;
   if (loglik_out) *loglik_out = ll;
   return TV_OK;
 }

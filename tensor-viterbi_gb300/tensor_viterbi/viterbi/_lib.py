@@ -23,6 +23,7 @@ TV_ENOMEM = -6
 TV_ECUDA = -7
 TV_EINTERNAL = -8
 TV_ENODEV = -9
+TV_ETIMEOUT = -10
 
 # Argument errors surface as ValueError (the caller passed something the
 # decoder cannot accept); runtime failures as RuntimeError.
@@ -45,7 +46,13 @@ EXPORTS = {
     "tv_decode_batch": (C.c_int, [C.c_void_p, C.c_int, _lp, _ip, _ip, _dp]),
     "tv_decode_batch_device": (C.c_int, [C.c_void_p, C.c_int, _lp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "tv_model_last_launches": (C.c_int64, [C.c_void_p]),
+    "tv_model_set_path": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "tv_model_last_path": (C.c_int, [C.c_void_p]),
 }
+
+TV_PATH_AUTO = 0
+TV_PATH_CTA = 1
+TV_PATH_GRID = 2
 
 
 def lib():

@@ -157,6 +157,17 @@ class Model:
     def last_launches(self) -> int:
         return int(_lib.lib().tv_model_last_launches(self._h))
 
+    def set_path(self, path: str = "auto", grid_ctas: int = 0) -> None:
+        """Kernel choice for single-sequence decodes: 'auto', 'cta' (one CTA,
+        window in its shared memory) or 'grid' (whole-GPU persistent grid);
+        grid_ctas > 0 caps the grid size.  Results are identical."""
+        code = {"auto": _lib.TV_PATH_AUTO, "cta": _lib.TV_PATH_CTA, "grid": _lib.TV_PATH_GRID}[path]
+        _lib.check(_lib.lib().tv_model_set_path(self._h, code, int(grid_ctas)))
+
+    def last_path(self) -> str:
+        return {_lib.TV_PATH_CTA: "cta", _lib.TV_PATH_GRID: "grid"}.get(
+            int(_lib.lib().tv_model_last_path(self._h)), "none")
+
 
 def decode_tensor_viterbi_cuda_loglik(n_states, trans_mat, emission_probs, duration_probs_linear,
                                       start_probs, duration_probs, obs_seq):

@@ -1,0 +1,95 @@
+"""GPU parity of the whole-GPU grid kernel (head CTA + worker CTAs): the same
+results as the oracle and as the one-CTA kernel, bit for bit, on the golden
+fixtures, on random shapes and at grid sizes from a handful of CTAs to one
+per SM."""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def _grid_ok(N, D):
+    return D > 4 and N <= 128
+
+
+@pytest.mark.parametrize("grid_ctas", [0, 5])
+@pytest.mark.parametrize("name", golden_names())
+def test_grid_golden(tvlib, name, grid_ctas):
+    args, z = load_golden(name)
+    N, D = args[0], args[5].shape[0]
+    if not _grid_ok(N, D):
+        pytest.skip("shape outside the grid kernel (D <= 4)")
+    ref = orc.decode(*args)
+    with tvlib.Model(*args[:6]) as m:
+        m.set_path("grid", grid_ctas)
+        path, ll = m.decode(args[6], return_loglik=True)
+        assert m.last_path() == "grid"
+    np.testing.assert_array_equal(path, z["path_cpp"])
+    assert ll == ref["loglik"]
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_grid_random_vs_oracle_and_cta(tvlib, seed):
+    import tensor_viterbi.synthetic as syn
+    rng = np.random.default_rng(500 + seed)
+    N = int(rng.integers(1, 60))
+    D = int(rng.integers(5, 400))
+    T = int(rng.integers(D, D + 2 * D + 300))
+    M = int(rng.integers(2, 32))
+    lo = float(rng.uniform(1, max(2, D / 3)))
+    hi = float(rng.uniform(lo, max(lo + 1, D)))
+    p = syn.discrete_problem(N, D, T, M, lo, hi, seed=seed)
+    ref = orc.decode(*p.args(), variant="omp")
+    with tvlib.Model(*p.model_args()) as m:
+        m.set_path("grid", int(rng.integers(2, 40)))
+        pg, lg = m.decode(p.obs_seq, return_loglik=True)
+        m.set_path("cta")
+        pc, lc = m.decode(p.obs_seq, return_loglik=True)
+    np.testing.assert_array_equal(pg, ref["path"])
+    np.testing.assert_array_equal(pc, ref["path"])
+    assert lg == ref["loglik"] == lc
+
+
+def test_grid_long_window_early_phase(tvlib):
+    """D in the thousands: the checkpointed newest-first sums (t <= D), the
+    switch to running folds at t = D+1 and a window spread over many CTAs."""
+    import tensor_viterbi.synthetic as syn
+    p = syn.discrete_problem(12, 2500, 5600, 24, 50.0, 1200.0, seed=77)
+    ref = orc.decode(*p.args(), variant="omp")
+    with tvlib.Model(*p.model_args()) as m:
+        path, ll = m.decode(p.obs_seq, return_loglik=True)
+        assert m.last_path() == "grid"
+    np.testing.assert_array_equal(path, ref["path"])
+    assert ll == ref["loglik"]
+
+
+def test_grid_gaussian_table(tvlib):
+    import tensor_viterbi.synthetic as syn
+    p = syn.gaussian_problem(20, 300, 2000, 10.0, 150.0, seed=5)
+    ref = orc.decode(*p.args(), variant="omp")
+    with tvlib.Model(*p.model_args()) as m:
+        m.set_path("grid", 0)
+        path, ll = m.decode(p.obs_seq, return_loglik=True)
+    np.testing.assert_array_equal(path, ref["path"])
+    assert ll == ref["loglik"]
+
+
+def test_grid_device_obs_validation(tvlib):
+    import torch
+    import tensor_viterbi.synthetic as syn
+    p = syn.discrete_problem(8, 50, 400, 6, 5.0, 30.0, seed=3)
+    ref = orc.decode(*p.args())
+    with tvlib.Model(*p.model_args()) as m:
+        m.set_path("grid", 6)
+        bad = torch.from_numpy(p.obs_seq.copy()).cuda()
+        bad[123] = 6
+        out = torch.empty_like(bad)
+        m.decode_device(bad.data_ptr(), bad.numel(), out.data_ptr(), 0, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        # the host-buffer call afterwards still works and is exact
+        path, ll = m.decode(p.obs_seq, return_loglik=True)
+    np.testing.assert_array_equal(path, ref["path"])
+    assert ll == ref["loglik"]
