@@ -1,0 +1,336 @@
+#!/usr/bin/env python3
+"""HSMM Viterbi decode benchmark on GB300: T*N*D cells per second.
+
+Default workload: one long sequence, N=75 states, max duration D=5000,
+T=1,000,000 observations over M=32 symbols, duration means ~U[50, 2500]
+(seeded synthetic model of the benchmark family; the reference publishes no
+dataset for this shape).  A "step" is one full decode of that sequence.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value   device time of K decodes with the inputs resident in HBM, L2 flushed
+        (256 MiB write) between decodes, CUDA events on the decode stream;
+        max over ranks; whole-job cells/s.
+e2e     the reference-facing call decode_tensor_viterbi_cuda(...) with host
+        numpy buffers: model preparation and upload, observation H2D, decode,
+        path D2H, all inside the timed region.
+roofline the grid decode kernel's algorithmic bytes (24 B per T*N*D cell:
+        window score, emission window sum and duration log-pmf, FP64) over its
+        event-timed duration, against the measured HBM copy bandwidth.
+cpu_baseline / --impl reference: the CPU restatement of the reference's
+        OpenMP decoder (oracle/, -O3 -ffast-math) on the host's cores, on a
+        bounded T-prefix of the same workload.
+Under torchrun (N > 1) every rank decodes its own replica: a single sequence
+does not shard (each step needs the whole previous score vector).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = pathlib.Path(__file__).resolve().parent
+PKG = REPO / "tensor-viterbi_gb300"
+for _p in (str(REPO), str(PKG)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+ALGO_BYTES_PER_CELL = 24
+METRIC = "T*N*D cells/s (HSMM Viterbi decode, FP64 log space, exact paths)"
+
+WORKLOADS = {
+    "single_N75_D5000_T1e6": dict(N=75, D=5000, T=1_000_000, M=32, lo=50.0, hi=2500.0, seed=1),
+    "single_N10_D100_T1e3": dict(N=10, D=100, T=1000, M=16, lo=5.0, hi=50.0, seed=0),
+    "single_N100_D10000_T1e6": dict(N=100, D=10_000, T=1_000_000, M=64, lo=5.0, hi=50.0, seed=4),
+}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_problem(w):
+    import tensor_viterbi.synthetic as syn
+    return syn.discrete_problem(w["N"], w["D"], w["T"], w["M"], w["lo"], w["hi"], seed=w["seed"])
+
+
+def measured_peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def committed_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch from a committed ncu summary, if there is one."""
+    p = REPO / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    try:
+        d = json.loads(p.read_text())
+        return d.get(kernel, {}).get(workload)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append(dict(sm=float(parts[1]), smax=float(parts[2]), reasons=parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        active = sorted({names[k] for r in rows for k in range(4) if r["reasons"][k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(r["sm"] for r in rows), "sm_max_mhz": max(r["smax"] for r in rows),
+                "reasons": active, "samples": len(rows)}
+
+
+def cpu_sample(prob, w, threads: int, max_extra: int = 200):
+    """The oracle's OpenMP decoder on the T-prefix D + max_extra of the
+    workload.  Returns (cells/s, seconds, T_sample)."""
+    from oracle import oracle as orc
+    Ts = min(w["T"], w["D"] + max_extra)
+    args = prob.model_args() + (prob.obs_seq[:Ts],)
+    t0 = time.perf_counter()
+    orc.decode(*args, variant="omp", nthreads=threads, fast=True)
+    dt = time.perf_counter() - t0
+    return Ts * w["N"] * w["D"] / dt, dt, Ts
+
+
+def run_reference(args, w, wname):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle as orc
+    orc.build()
+    threads = orc.cpu_count()
+    prob = make_problem(w)
+    for _ in range(args.warmup):
+        cpu_sample(prob, w, threads)
+    vals, secs = [], []
+    for _ in range(args.steps):
+        v, dt, Ts = cpu_sample(prob, w, threads)
+        vals.append(v)
+        secs.append(dt)
+    value = Ts * w["N"] * w["D"] * len(secs) / sum(secs)
+    sample = (f"T-prefix {Ts} of the workload ({Ts * w['N'] * w['D']:.3e} cells) per step, "
+              f"OpenMP restatement of src/hsmm.cu:376-600, {threads} threads")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_of(w, wname, ws),
+        "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def config_of(w, wname, ws):
+    return {"workload": wname, "n_states": w["N"], "max_dur": w["D"], "T": w["T"], "symbols": w["M"],
+            "duration_means": f"U[{w['lo']:g},{w['hi']:g}]", "seed": w["seed"],
+            "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{ws}",
+            "form": "single sequence"}
+
+
+def run_ours(args, w, wname):
+    import numpy as np
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    from tensor_viterbi.viterbi import native
+    native.configure("gb300", "cuda")
+    prob = make_problem(w)
+    N, D, T = w["N"], w["D"], w["T"]
+    cells = T * N * D
+
+    model = native.Model(*prob.model_args())
+    model.set_timing(True)
+    obs = torch.from_numpy(prob.obs_seq).to(dev)
+    path = torch.empty_like(obs)
+    ll = torch.zeros(1, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def one_decode():
+        flush.fill_(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        model.decode_device(obs.data_ptr(), T, path.data_ptr(), ll.data_ptr(), stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1), model.kernel_ms(), model.last_launches()
+
+    for _ in range(args.warmup):
+        one_decode()
+    barrier(ws)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    t_wall = time.perf_counter()
+    step_ms, kern_ms, launches = [], [], 0
+    for _ in range(args.steps):
+        a, k, n = one_decode()
+        step_ms.append(a)
+        kern_ms.append(k)
+        launches += n
+    torch.cuda.synchronize()
+    barrier(ws)
+    wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    total_ms = max_over_ranks(sum(step_ms), ws)
+    value = cells * args.steps * ws / (total_ms / 1e3)
+
+    # Roofline of the grid decode kernel (events on its own stream).
+    peak, peak_kind = measured_peaks()
+    kmean = statistics.mean(kern_ms) if kern_ms and min(kern_ms) > 0 else float("nan")
+    achieved = ALGO_BYTES_PER_CELL * cells / (kmean / 1e3) / 1e9
+    traffic = committed_traffic("grid_decode_kernel", wname)
+
+    # e2e: the drop-in call with host buffers, copies inside the timed region.
+    args_host = prob.args()
+    for _ in range(max(1, min(args.warmup, 2))):
+        native.decode_tensor_viterbi_cuda(*args_host)
+    barrier(ws)
+    e2e_s = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        p_host, ll_host = native.decode_tensor_viterbi_cuda_loglik(*args_host)
+        e2e_s.append(time.perf_counter() - t0)
+    e2e_total = max_over_ranks(sum(e2e_s), ws)
+    e2e_value = cells * args.steps * ws / e2e_total
+    h2d = (N * N + prob.O * N + N + 2 * D * N) * 8 + T * 4
+    d2h = T * 4 + 8 + 16
+
+    # The timed device-resident decode and the drop-in call must agree.
+    same = bool(np.array_equal(path.cpu().numpy(), p_host)) and float(ll.item()) == ll_host
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            from oracle import oracle as orc
+            orc.build()
+            threads = orc.cpu_count()
+            v, dt, Ts = cpu_sample(prob, w, threads)
+            cpu = {"value": v, "unit": "cells/s", "cores": threads, "kind": "port",
+                   "sample": f"T-prefix {Ts} ({Ts * N * D:.3e} cells, {dt:.1f} s), OpenMP restatement of "
+                             f"src/hsmm.cu:376-600 built -O3 -ffast-math, {threads} threads"}
+        line = {
+            "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_of(w, wname, ws),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "grid_decode_kernel", "kernel_ms": kmean,
+                         "algo_bytes_per_launch": ALGO_BYTES_PER_CELL * cells, "peak_source": peak_kind},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "cells/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": 1e3 * e2e_total / args.steps},
+            "gpu_launches": launches,
+            "clocks": clk,
+            "kernel_path": model.last_path(),
+            "wall_s": wall,
+            "consistent": same,
+            "loglik": ll_host,
+        }
+        print(json.dumps(line), flush=True)
+    model.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="single_N75_D5000_T1e6")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, w, args.workload)
+    return run_ours(args, w, args.workload)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -115,6 +115,13 @@ int tv_model_set_path(tv_model m, int path, int grid_ctas);
  * TV_PATH_GRID). */
 int tv_model_last_path(tv_model m);
 
+/* Kernel timing for benchmark reporting (no reference counterpart).  When
+ * enabled, CUDA events on the decode's own stream bracket its main kernel;
+ * tv_model_kernel_ms waits for that kernel and returns its time in ms for
+ * the most recent decode, or a negative value when none was recorded. */
+int tv_model_set_timing(tv_model m, int enable);
+double tv_model_kernel_ms(tv_model m);
+
 #ifdef __cplusplus
 }
 #endif

@@ -125,6 +125,9 @@ struct tv_model_s {
   int plan_key_N = -1, plan_key_D = -1, plan_key_G = -1;
   tv::GridParams plan{};
   int path_pref = TV_PATH_AUTO, grid_ctas = 0, last_path = 0;
+  // optional events around the main kernel
+  bool timing = false, timed = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::mutex mu;
 };
 
@@ -159,6 +162,15 @@ Quant choose_quant(const tv_model_s* m, int64_t T) {
   Q.scale = std::ldexp(1.0, f);
   Q.margin = (long long)std::ceil(2.0 * err * Q.scale) + 8;
   return Q;
+}
+
+void mark_start(tv_model_s* m, cudaStream_t st) {
+  m->timed = false;
+  if (m->timing && m->ev0) cudaEventRecord(m->ev0, st);
+}
+
+void mark_end(tv_model_s* m, cudaStream_t st) {
+  if (m->timing && m->ev1 && cudaEventRecord(m->ev1, st) == cudaSuccess) m->timed = true;
 }
 
 int prepare_quant(tv_model_s* m, const Quant& Q, cudaStream_t st) {
@@ -252,8 +264,10 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
   bv.status = m->status.p;
   bv.next = m->counter.p;
   bv.n_seq = n_seq;
+  mark_start(m, st);
   kern<<<grid, kThreads, dyn, st>>>(view(m, Q), bv, L, scratch);
   TV_CUDA(cudaGetLastError());
+  mark_end(m, st);
   m->last_launches += 1;
   return TV_OK;
 }
@@ -372,7 +386,9 @@ int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_
   void* args[] = {&mv, &Pc, &B};
   const size_t dyn = std::max(P.w_bytes, P.h_bytes);
   TV_CUDA(cudaFuncSetAttribute(tv::grid_decode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  mark_start(m, st);
   TV_CUDA(cudaLaunchCooperativeKernel((void*)tv::grid_decode_kernel, dim3(P.G), dim3(tv::GRID_THREADS), args, dyn, st));
+  mark_end(m, st);
   m->last_launches += 1;
   return TV_OK;
 }
@@ -513,6 +529,8 @@ int tv_model_destroy(tv_model m) {
   m->slot_ctil.release(); m->slot_itil.release(); m->slot_dsel.release(); m->dstar_g.release();
   m->dinit.release(); m->ck.release(); m->part.release();
   m->seg_first.release(); m->seg_count.release(); m->seg_base.release(); m->gflags.release();
+  if (m->ev0) cudaEventDestroy(m->ev0);
+  if (m->ev1) cudaEventDestroy(m->ev1);
   m->obs_tmp.release(); m->path_tmp.release(); m->ll_tmp.release();
   delete m;
   return TV_OK;
@@ -529,6 +547,26 @@ int tv_model_set_path(tv_model m, int path, int grid_ctas) {
 }
 
 int tv_model_last_path(tv_model m) { return m ? m->last_path : 0; }
+
+int tv_model_set_timing(tv_model m, int enable) {
+  if (!m) return fail(TV_EINVAL, "null model");
+  std::lock_guard<std::mutex> lk(m->mu);
+  if (enable && !m->ev0) {
+    TV_CUDA(cudaEventCreate(&m->ev0));
+    TV_CUDA(cudaEventCreate(&m->ev1));
+  }
+  m->timing = enable != 0;
+  m->timed = false;
+  return TV_OK;
+}
+
+double tv_model_kernel_ms(tv_model m) {
+  if (!m || !m->timed) return -1.0;
+  if (cudaEventSynchronize(m->ev1) != cudaSuccess) return -1.0;
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, m->ev0, m->ev1) != cudaSuccess) return -1.0;
+  return (double)ms;
+}
 
 int tv_decode_device(tv_model m, const int32_t* obs_dev, int64_t T, int32_t* path_dev, double* ll_dev,
                      void* stream) {

@@ -164,6 +164,15 @@ class Model:
         code = {"auto": _lib.TV_PATH_AUTO, "cta": _lib.TV_PATH_CTA, "grid": _lib.TV_PATH_GRID}[path]
         _lib.check(_lib.lib().tv_model_set_path(self._h, code, int(grid_ctas)))
 
+    def set_timing(self, enable: bool = True) -> None:
+        """Bracket the main decode kernel with CUDA events on its stream."""
+        _lib.check(_lib.lib().tv_model_set_timing(self._h, 1 if enable else 0))
+
+    def kernel_ms(self) -> float:
+        """Main-kernel time of the most recent decode (waits for it); < 0 if
+        timing was off."""
+        return float(_lib.lib().tv_model_kernel_ms(self._h))
+
     def last_path(self) -> str:
         return {_lib.TV_PATH_CTA: "cta", _lib.TV_PATH_GRID: "grid"}.get(
             int(_lib.lib().tv_model_last_path(self._h)), "none")
