@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
           bi = i1;
         } else {
           const ExactBest eb = rescore_state(m, j, t, tau, r0, tb.b1 - m.margin, qd, ctil, acc, dstar, lane);
-          vbest = eb.v;
+          vbest = eb.value();
           bd = eb.d;
           bi = eb.i;
         }
@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
         eb.warp_reduce();
         if (lane == 0) {
           if (eb.d == IDX_NONE) { eb.d = 0; eb.i = 0; }
-          tail[j] = eb.v;
+          tail[j] = eb.value();
           psi[(size_t)t * N + j] = pack_psi(eb.d, eb.i);
         }
       }

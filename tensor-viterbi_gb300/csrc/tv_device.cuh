@@ -59,27 +59,44 @@ struct Top2 {
   }
 };
 
+// Order-preserving int64 image of a double: comparing keys as signed integers
+// orders finite values and -inf as the doubles compare (-0 is mapped to +0 so
+// that they tie, as in IEEE).  GB300 issues FP64 at 1/64 of the FP32 rate, so
+// exact comparisons run on the integer pipes through these keys.
+__device__ __forceinline__ long long order_key(double v) {
+  long long b = __double_as_longlong(v);
+  if (b == (long long)0x8000000000000000ULL) b = 0;
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double key_value(long long k) {
+  return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL));
+}
+constexpr long long KEY_NEG_INF = (long long)0x800fffffffffffffULL;  // order_key(-inf)
+
 // Exact candidate in the reference's order: the larger value wins, then the
 // lower d, then the lower i (the d-outer / i-inner strict '>' scan of
 // src/hsmm.cu:340-350).
 struct ExactBest {
-  double v;
+  long long k;  // order_key of the value
   int d;
   int i;
-  __device__ __forceinline__ void init() { v = -__longlong_as_double(0x7ff0000000000000LL); d = IDX_NONE; i = IDX_NONE; }
-  __device__ __forceinline__ bool better(double ov, int od, int oi) const {
-    return (ov > v) || (ov == v && (od < d || (od == d && oi < i)));
+  __device__ __forceinline__ void init() { k = KEY_NEG_INF; d = IDX_NONE; i = IDX_NONE; }
+  __device__ __forceinline__ double value() const { return key_value(k); }
+  __device__ __forceinline__ void set(double v, int od, int oi) { k = order_key(v); d = od; i = oi; }
+  __device__ __forceinline__ bool better_key(long long ok, int od, int oi) const {
+    return (ok > k) || (ok == k && (od < d || (od == d && oi < i)));
   }
-  __device__ __forceinline__ void offer(double ov, int od, int oi) {
-    if (better(ov, od, oi)) { v = ov; d = od; i = oi; }
+  __device__ __forceinline__ void offer_key(long long ok, int od, int oi) {
+    if (better_key(ok, od, oi)) { k = ok; d = od; i = oi; }
   }
+  __device__ __forceinline__ void offer(double v, int od, int oi) { offer_key(order_key(v), od, oi); }
   __device__ __forceinline__ void warp_reduce() {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const double ov = __shfl_xor_sync(0xffffffffu, v, o);
+      const long long ok = __shfl_xor_sync(0xffffffffu, k, o);
       const int od = __shfl_xor_sync(0xffffffffu, d, o);
       const int oi = __shfl_xor_sync(0xffffffffu, i, o);
-      offer(ov, od, oi);
+      offer_key(ok, od, oi);
     }
   }
 };

@@ -9,17 +9,21 @@
 //
 // Per step t:
 //   head    the serial critical path, all in its own shared memory: the N x N
-//           max-plus matvec for the newest slot s = t-1 (published to the
-//           workers), the candidates d < L, the merge with the workers'
-//           exact partial winners, the initialisation rule for t < D, the
-//           exact delta[t] and the back-pointers.
-//   workers for their cells: the exact window fold (t > D), the fixed-point
-//           scan over d >= L, the certified exact local winner, published
-//           as a tagged message.  A worker needs slot t-1-L to run step t,
-//           so it may run up to L steps ahead of the head; the cross-SM
-//           latency is overlapped instead of paid every step.
-// After step T-1 the tail (survival in place of the duration pmf) is one
-// more round of the same protocol with an exhaustive exact scan, and the head
+//           max-plus matvec for the newest slot s = t-1 (sent to the workers),
+//           the candidates d < L, the merge with the workers' exact partial
+//           winners, the initialisation rule for t < D, the exact delta[t]
+//           and the back-pointers.
+//   workers for their cells: the fixed-point scan over d >= L, the certified
+//           exact local winner (sent to the head), and, overlapped with it,
+//           the exact window folds of step t+1 (double-buffered).  A worker
+//           needs slot t-1-L to run step t, so it runs up to L steps ahead of
+//           the head and the cross-SM latency is overlapped, not paid per
+//           step.
+// Every cross-CTA value travels as tagged 64-bit words (tv_sync.cuh): a reader
+// that sees the expected tag holds the value, so no fence or flag round trip
+// sits on any per-step path.
+// After step T-1 the tail (survival in place of the duration pmf) is one more
+// round of the same protocol with an exhaustive exact scan; the head then
 // backtraces.
 //
 // While t <= D the reference rebuilds the window sums newest-first
@@ -33,11 +37,13 @@
 
 namespace tv {
 
-constexpr int GRID_THREADS = 1024;
-constexpr int GRID_L = 4;          // head candidates d < L
+constexpr int GRID_THREADS = 1024;   // the head uses all of them
+constexpr int WORKER_THREADS = 256;  // a worker CTA keeps 8 warps; the rest exit at once
+constexpr int GRID_L = 4;            // head candidates d < L (a power of two)
 constexpr int CK_STRIDE = 32;      // checkpoint stride of the early window sums
 constexpr int PART_RING = 32;      // steps of worker partials in flight
-constexpr int SLOT_RING = 64;      // published slot records kept
+constexpr int SLOT_RING = 64;      // slot messages kept
+constexpr int SLOT_WORDS = 5;      // ctil (2), dsel (2), itil (1)
 constexpr int HEAD_GROUP = 8;      // lanes per state in the head
 constexpr int GRID_MAX_N = GRID_THREADS / HEAD_GROUP;
 constexpr int EMPTY_D = 0xffff;
@@ -45,33 +51,32 @@ constexpr int TV_ETIMEOUT_DEV = -10;
 
 struct GridParams {
   int G, L, S, Rd, M;
-  long long chunk;
+  long long chunk;  // largest worker range, in cells
   int max_seg;
-  unsigned long long w_qd, w_ctil, w_dsel, w_acc, w_itil, w_red, w_bytes;
+  unsigned long long w_qd, w_dur, w_tr, w_ctil, w_dsel, w_acc0, w_acc1, w_itil, w_red, w_bytes;
   unsigned long long h_qtr, h_ctil, h_itil, h_dstar, h_E, h_qd, h_dur, h_dq, h_ptil, h_pv, h_pd, h_pi, h_tail,
-      h_red, h_bytes;
+      h_bytes;
   long long timeout;
 };
 
 struct GridBufs {
   const int32_t* obs;
   long long T;
-  uint32_t* psi;               // (T, N)
-  int32_t* path;               // (T)
-  double* loglik;              // (1) or null
-  long long* slot_ctil;        // [SLOT_RING][N]
-  unsigned short* slot_itil;   // [SLOT_RING][N]
-  double* slot_dsel;           // [SLOT_RING][N] exact delta[s][argmax i]
-  unsigned long long* part;    // [PART_RING][S][3] tagged messages
-  double* dstar_g;             // [Rd][N] exact delta ring
-  const double* dinit;         // [D][N] initialisation scores
-  const double* ck;            // [D][M][N] checkpoints of the early window sums
-  const int* seg_first;        // [N]
-  const int* seg_count;        // [N]
-  const int* seg_base;         // [G-1]
-  unsigned* pub;               // number of slots the head has published
+  uint32_t* psi;                // (T, N)
+  int32_t* path;                // (T)
+  double* loglik;               // (1) or null
+  unsigned long long* slot_msg; // [SLOT_RING][N][5] tagged slot records
+  unsigned long long* part;     // [PART_RING][S][3] tagged partial winners
+  unsigned long long* dstar;    // [Rd][N][2] tagged exact delta ring
+  const double* dinit;          // [D][N] initialisation scores
+  const double* ck;             // [D][M][N] checkpoints of the early window sums
+  const long long* wrange;      // [G-1][2] worker cell ranges
+  const int* seg_first;         // [N]
+  const int* seg_count;         // [N]
+  const int* seg_base;          // [G-1]
   int* abort_flag;
   int* status;
+  int* site;                    // which wait gave up (diagnostics)
 };
 
 // g_t(d) = em_t + em_{t-1} + ... + em_{t-d}, folded newest-first like the
@@ -123,137 +128,126 @@ __global__ void grid_prep_ck(ModelView m, const int32_t* obs, double* ck, int M,
   }
 }
 
-__device__ __forceinline__ void grid_fail(const GridBufs& B, int code) {
+// Wait sites reported with a timeout.
+enum { SITE_HEAD_PARTIAL = 1, SITE_WORKER_SLOT = 2, SITE_WORKER_RESCORE = 3, SITE_WORKER_TAIL = 4,
+       SITE_HEAD_TAIL = 5 };
+
+__device__ __forceinline__ void grid_fail(const GridBufs& B, int code, int site) {
+  if (atomicCAS(B.status, 0, code) == 0) *B.site = site;
   atomicExch(B.abort_flag, 1);
-  atomicCAS(B.status, 0, code);
 }
 
-// Block-wide reduction of an ExactBest; every thread receives the result.
-__device__ __forceinline__ ExactBest block_reduce_exact(ExactBest eb, ExactBest* scratch) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+// Exact delta[s][i] from the tagged ring (tag s+1), as an order key.
+__device__ __forceinline__ bool load_dstar(const GridBufs& B, const GridParams& P, int N, long long s, int i,
+                                           double& v) {
+  unsigned long long bits;
+  if (!tagged64_load(B.dstar + ((size_t)(s % P.Rd) * N + i) * 2, (unsigned)(s + 1), bits, B.abort_flag, P.timeout))
+    return false;
+  v = __longlong_as_double((long long)bits);
+  return true;
+}
+
+// Named barrier of the worker threads only (the rest of the CTA has exited).
+__device__ __forceinline__ void worker_sync() {
+  asm volatile("bar.sync 1, %0;" ::"r"(WORKER_THREADS) : "memory");
+}
+
+// Block-wide reduction of an ExactBest over the worker threads; every worker
+// thread receives the result.
+__device__ __forceinline__ ExactBest worker_reduce_exact(ExactBest eb, ExactBest* scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   eb.warp_reduce();
-  __syncthreads();
+  worker_sync();
   if (lane == 0) scratch[warp] = eb;
-  __syncthreads();
+  worker_sync();
   ExactBest r;
   r.init();
-  if (lane < nw) r = scratch[lane];
+  if (lane < WORKER_THREADS / 32) r = scratch[lane];
   r.warp_reduce();
   return r;
 }
 
+__device__ __forceinline__ void send_partial(const GridBufs& B, const GridParams& P, unsigned tag, unsigned ring,
+                                             int seg, const ExactBest& eb) {
+  TaggedMsg msg;
+  const bool empty = eb.d == IDX_NONE;
+  msg_pack(msg, tag, eb.value(), empty ? EMPTY_D : eb.d, empty ? 0 : eb.i);
+  msg_store(B.part + ((size_t)ring * P.S + seg) * 3, msg);
+}
+
 // ---------------------------------------------------------------------------
-// Worker CTA
+// Worker CTA (WORKER_THREADS threads)
 // ---------------------------------------------------------------------------
 __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridBufs& B, unsigned char* sm) {
-  const int N = m.N, D = m.D, L = P.L;
+  constexpr int L = GRID_L;
+  constexpr int NW = WORKER_THREADS / 32;
+  const int N = m.N, D = m.D;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int w = blockIdx.x - 1;
-  const long long ND = (long long)N * D;
-  const long long c_lo = (long long)w * P.chunk;
-  const long long c_hi = c_lo + P.chunk < ND ? c_lo + P.chunk : ND;
-  if (c_lo >= c_hi) return;  // idle worker: owns no cells, publishes nothing
+  const long long c_lo = B.wrange[2 * w], c_hi = B.wrange[2 * w + 1];
+  if (c_lo >= c_hi) return;  // idle worker: owns no cells, sends nothing
   const int ja = (int)(c_lo / D), jb = (int)((c_hi - 1) / D);
   const int nseg = jb - ja + 1;
   const int off0 = (int)(c_lo - (long long)ja * D);  // ring slot of the first cell
   const int seg0 = B.seg_base[w];
   const long long T = B.T;
-  long long* qd = (long long*)(sm + P.w_qd);
-  long long* ctil = (long long*)(sm + P.w_ctil);
-  double* dsel = (double*)(sm + P.w_dsel);
-  double* acc = (double*)(sm + P.w_acc);
+  long long* qd = (long long*)(sm + P.w_qd);          // [nseg][D]
+  double* dur = (double*)(sm + P.w_dur);              // [nseg][D]
+  double* tr = (double*)(sm + P.w_tr);                // [nseg][N]
+  long long* ctil = (long long*)(sm + P.w_ctil);      // [ncell]
+  double* dsel = (double*)(sm + P.w_dsel);            // [ncell]
+  double* acc_cur = (double*)(sm + P.w_acc0);         // [ncell] E_t
+  double* acc_nxt = (double*)(sm + P.w_acc1);         // [ncell] E_{t+1}
   unsigned short* itil = (unsigned short*)(sm + P.w_itil);
-  Top2* red = (Top2*)(sm + P.w_red);  // [max_seg][32]
+  Top2* red = (Top2*)(sm + P.w_red);                  // [nseg][NW]
   ExactBest* ered = (ExactBest*)(sm + P.w_red);
-  __shared__ int s_ok;
-  __shared__ unsigned s_pub;
+  __shared__ int s_bad;
 
-  for (long long k = tid; k < (long long)nseg * D; k += blockDim.x) qd[k] = m.qdurT[(size_t)ja * D + k];
-  unsigned pub_seen = 0;
-  __syncthreads();
+  for (long long k = tid; k < (long long)nseg * D; k += WORKER_THREADS) {
+    qd[k] = m.qdurT[(size_t)ja * D + k];
+    dur[k] = m.durT[(size_t)ja * D + k];
+  }
+  for (int k = tid; k < nseg * N; k += WORKER_THREADS) tr[k] = m.trans[(size_t)ja * N + k];
+  if (tid == 0) s_bad = 0;
+  worker_sync();
 
-  auto seg_range = [&](int s, int& rb, int& re) {
+  auto seg_of = [&](int s, int& rb, int& re) {
     rb = (s == 0) ? off0 : 0;
     re = (s == nseg - 1) ? (int)(c_hi - (long long)jb * D) : D;
   };
 
+  int r0 = 0;  // (t-1) % D
   for (long long t = 1; t < T; ++t) {
     const int tau = (int)(t < D ? t : D);
-    const int r0 = (int)((t - 1) % D);
-    const long long s_new = t - 1 - L;
+    const unsigned prow = (unsigned)t & (PART_RING - 1);
 
-    // Intake of the slot record that enters the worker domain (d = L).
-    if (s_new >= 0) {
-      if (pub_seen < (unsigned)(s_new + 1)) {
-        if (tid == 0) {
-          unsigned seen = 0;
-          s_ok = wait_geq(B.pub, (unsigned)(s_new + 1), seen, B.abort_flag, P.timeout) ? 1 : 0;
-          s_pub = seen;
-          if (!s_ok) grid_fail(B, TV_ETIMEOUT_DEV);
-        }
-        __syncthreads();
-        if (!s_ok) return;
-        pub_seen = s_pub;
-      }
-      const int r_new = (int)(s_new % D);
-      if (tid < nseg) {
-        int rb, re;
-        seg_range(tid, rb, re);
-        if (r_new >= rb && r_new < re) {
-          const int j = ja + tid;
-          const int c = tid * D + r_new - off0;
-          const size_t rec = (size_t)(s_new % SLOT_RING) * N + j;
-          ctil[c] = __ldcg(B.slot_ctil + rec);
-          itil[c] = __ldcg(B.slot_itil + rec);
-          dsel[c] = __ldcg(B.slot_dsel + rec);
-        }
-      }
-    }
-    // First step past D: seed the running folds with the reference's
-    // newest-first window sums of step D (slot s = r has d = D-1-r then).
-    if (t == D + 1) {
-      for (int s = 0; s < nseg; ++s) {
-        int rb, re;
-        seg_range(s, rb, re);
-        for (int r = rb + tid; r < re; r += blockDim.x)
-          acc[s * D + r - off0] = early_window(m, B.ck, P.M, B.obs, D, D - 1 - r, ja + s);
-      }
-    }
-    __syncthreads();
-
-    // Window fold (t > D) and fixed-point scan over d in [L, tau).
-    const int ot = B.obs[t];
+    // Phase 1: fixed-point scan over d in [L, tau).
     for (int s = 0; s < nseg; ++s) {
       int rb, re;
-      seg_range(s, rb, re);
-      const int j = ja + s;
-      const double emj = m.em[(size_t)ot * N + j];
+      seg_of(s, rb, re);
+      const long long* ct = ctil + s * D - off0;
+      const long long* q = qd + s * D;
       Top2 tb;
       tb.init();
-      for (int r = rb + tid; r < re; r += blockDim.x) {
-        const int c = s * D + r - off0;
+      for (int r = rb + tid; r < re; r += WORKER_THREADS) {
         int d = r0 - r;
         if (d < 0) d += D;
-        if (t > D) {
-          const double a = (d == 0) ? 0.0 : acc[c];
-          acc[c] = a + emj;
-        }
-        if (d >= L && d < tau) tb.push(ctil[c] + qd[s * D + d], d);
+        if (d >= L && d < tau) tb.push(ct[r] + q[d], d);
       }
       tb.warp_reduce();
-      if (lane == 0) red[s * 32 + warp] = tb;
+      if (lane == 0) red[s * NW + warp] = tb;
     }
-    __syncthreads();
+    worker_sync();
 
-    // Certified exact winner per segment, published as a tagged message.
-    if (warp < nseg) {
-      const int s = warp;
+    // Phase 2a: certified exact winner per segment (warps take segments in
+    // turn), sent to the head.
+    for (int s = warp; s < nseg; s += NW) {
       const int j = ja + s;
       int rb, re;
-      seg_range(s, rb, re);
+      seg_of(s, rb, re);
       Top2 tb;
       tb.init();
-      if (lane < (int)(blockDim.x >> 5)) tb = red[s * 32 + lane];
+      if (lane < NW) tb = red[s * NW + lane];
       tb.warp_reduce();
       ExactBest eb;
       eb.init();
@@ -265,34 +259,118 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
         const unsigned short it = itil[c1];
         const bool amb = (it & 0x8000) || ((tb.b1 - tb.b2) <= m.margin);
         if (!amb) {
-          const int i1 = it & 0x7fff;
-          const double e = (t > D) ? acc[c1] : early_window(m, B.ck, P.M, B.obs, t, d1, j);
-          const double v = (e + dsel[c1]) + (m.trans[(size_t)j * N + i1] + m.durT[(size_t)j * D + d1]);
-          eb.v = v; eb.d = d1; eb.i = i1;
+          if (lane == 0) {
+            const int i1 = it & 0x7fff;
+            const double e = (t > D) ? acc_cur[c1] : early_window(m, B.ck, P.M, B.obs, t, d1, j);
+            eb.set((e + dsel[c1]) + (tr[s * N + i1] + dur[s * D + d1]), d1, i1);
+          }
         } else {
+          // Re-score every candidate inside the margin exactly.
           const long long thr = tb.b1 - m.margin;
+          bool ok = true;
           for (int r = rb + lane; r < re; r += 32) {
-            const int c = s * D + r - off0;
             int d = r0 - r;
             if (d < 0) d += D;
             if (d < L || d >= tau) continue;
+            const int c = s * D + r - off0;
             if (ctil[c] + qd[s * D + d] < thr) continue;
-            const double e = (t > D) ? acc[c] : early_window(m, B.ck, P.M, B.obs, t, d, j);
-            const double du = m.durT[(size_t)j * D + d];
-            const double* row = B.dstar_g + (size_t)((t - 1 - d) % P.Rd) * N;
-            const double* tr = m.trans + (size_t)j * N;
-            for (int i = 0; i < N; ++i) eb.offer((e + __ldcg(row + i)) + (tr[i] + du), d, i);
+            const double e = (t > D) ? acc_cur[c] : early_window(m, B.ck, P.M, B.obs, t, d, j);
+            const double du = dur[s * D + d];
+            for (int i = 0; i < N && ok; ++i) {
+              double dv;
+              ok = load_dstar(B, P, N, t - 1 - d, i, dv);
+              if (ok) eb.offer((e + dv) + (tr[s * N + i] + du), d, i);
+            }
           }
           eb.warp_reduce();
+          if (!__all_sync(0xffffffffu, ok)) {
+            if (lane == 0) { grid_fail(B, TV_ETIMEOUT_DEV, SITE_WORKER_RESCORE); s_bad = 1; }
+          }
         }
       }
-      if (lane == 0) {
-        TaggedMsg msg;
-        msg_pack(msg, (unsigned)t, eb.v, eb.d == IDX_NONE ? EMPTY_D : eb.d, eb.d == IDX_NONE ? 0 : eb.i);
-        msg_store(B.part + ((size_t)(t % PART_RING) * P.S + seg0 + s) * 3, msg);
+      if (lane == 0) send_partial(B, P, (unsigned)t, prow, seg0 + s, eb);
+    }
+    // Phase 2b: intake of the slot that enters the worker domain at step t+1
+    // (s' = t-L, d = L then); the last warp, one lane per segment.  Lane 0
+    // waits for the slot message even when the slot is not its own: that is
+    // the flow control that keeps a worker at most L steps ahead of the head
+    // (its partials ring holds PART_RING steps).
+    if (warp == NW - 1 && lane < nseg && t + 1 < T && t - L >= 0) {
+      const long long sp = t - L;
+      int rn = r0 + 1 - L;
+      if (rn < 0) rn += D;
+      int rb, re;
+      seg_of(lane, rb, re);
+      const unsigned tag = (unsigned)(sp + 1);
+      const unsigned long long* msg =
+          B.slot_msg + ((size_t)((unsigned)sp & (SLOT_RING - 1)) * N + ja + lane) * SLOT_WORDS;
+      unsigned long long cbits, dbits, ibits;
+      if (rn < rb || rn >= re) {
+        if (lane == 0 && !tagged64_load(msg, tag, cbits, B.abort_flag, P.timeout)) {
+          grid_fail(B, TV_ETIMEOUT_DEV, SITE_WORKER_SLOT);
+          s_bad = 1;
+        }
+      } else {
+        bool ok = tagged64_load(msg, tag, cbits, B.abort_flag, P.timeout) &&
+                  tagged64_load(msg + 2, tag, dbits, B.abort_flag, P.timeout);
+        if (ok) {
+          unsigned long long iw = ld_relaxed_u64(msg + 4);
+          const long long t0 = clock64();
+          while ((unsigned)(iw >> 32) != tag) {
+            if (ld_relaxed_i32(B.abort_flag) || clock64() - t0 > P.timeout) { ok = false; break; }
+            iw = ld_relaxed_u64(msg + 4);
+          }
+          ibits = iw;
+        }
+        if (ok) {
+          const int c = lane * D + rn - off0;
+          ctil[c] = (long long)cbits;
+          dsel[c] = __longlong_as_double((long long)dbits);
+          itil[c] = (unsigned short)(ibits & 0xffff);
+        } else {
+          grid_fail(B, TV_ETIMEOUT_DEV, SITE_WORKER_SLOT);
+          s_bad = 1;
+        }
       }
     }
-    __syncthreads();
+    // Phase 2c: exact window folds of step t+1 into the other buffer,
+    // E_{t+1}[d] = E_t[d-1] + em_{t+1}, E_{t+1}[0] = 0 + em_{t+1}
+    // (src/hsmm.cu:298-310); at t+1 = D+1 seeded from the reference's
+    // newest-first sums of step D.
+    int r0n = r0 + 1;
+    if (r0n == D) r0n = 0;
+    const long long t1 = t + 1;
+    const bool fold = (t1 < T) && (t1 > D);
+    if (fold) {
+      const int ot1 = B.obs[t1];
+      for (int s = 0; s < nseg; ++s) {
+        int rb, re;
+        seg_of(s, rb, re);
+        const int j = ja + s;
+        const double em1 = m.em[(size_t)ot1 * N + j];
+        const double* ac = acc_cur + s * D - off0;
+        double* an = acc_nxt + s * D - off0;
+        if (t1 == D + 1) {
+          for (int r = rb + tid; r < re; r += WORKER_THREADS) {
+            int d = r0n - r;
+            if (d < 0) d += D;
+            const double base = (d == 0) ? 0.0 : early_window(m, B.ck, P.M, B.obs, D, d - 1, j);
+            an[r] = base + em1;
+          }
+        } else {
+          for (int r = rb + tid; r < re; r += WORKER_THREADS)
+            an[r] = ((r == r0n) ? 0.0 : ac[r]) + em1;
+        }
+      }
+    }
+    worker_sync();
+    if (s_bad) return;
+    if (fold) {
+      double* x = acc_cur;
+      acc_cur = acc_nxt;
+      acc_nxt = x;
+    }
+    r0 = r0n;
   }
 
   // Tail at t = T-1: exhaustive exact scan of the worker's cells with the
@@ -300,39 +378,44 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
   {
     const long long t = T - 1;
     const int tau = (int)(t < D ? t : D);
-    const int r0 = t >= 1 ? (int)((t - 1) % D) : 0;
+    const int rt = t >= 1 ? (int)((t - 1) % D) : 0;
     for (int s = 0; s < nseg; ++s) {
       int rb, re;
-      seg_range(s, rb, re);
+      seg_of(s, rb, re);
       const int j = ja + s;
       ExactBest eb;
       eb.init();
-      for (int r = rb + tid; r < re; r += blockDim.x) {
-        const int c = s * D + r - off0;
-        int d = r0 - r;
+      bool ok = true;
+      for (int r = rb + tid; r < re && ok; r += WORKER_THREADS) {
+        int d = rt - r;
         if (d < 0) d += D;
         if (d < L || d >= tau) continue;
-        const double E = (t > D) ? acc[c] : early_window(m, B.ck, P.M, B.obs, t, d, j);
+        const int c = s * D + r - off0;
+        const double E = (t > D) ? acc_cur[c] : early_window(m, B.ck, P.M, B.obs, t, d, j);
         const double e = E + m.survT[(size_t)j * D + d];
-        const double* row = B.dstar_g + (size_t)((t - 1 - d) % P.Rd) * N;
-        const double* tr = m.trans + (size_t)j * N;
-        for (int i = 0; i < N; ++i) eb.offer((e + __ldcg(row + i)) + tr[i], d, i);
+        for (int i = 0; i < N && ok; ++i) {
+          double dv;
+          ok = load_dstar(B, P, N, t - 1 - d, i, dv);
+          if (ok) eb.offer((e + dv) + tr[s * N + i], d, i);
+        }
       }
-      eb = block_reduce_exact(eb, ered);
-      if (tid == 0) {
-        TaggedMsg msg;
-        msg_pack(msg, (unsigned)T, eb.v, eb.d == IDX_NONE ? EMPTY_D : eb.d, eb.d == IDX_NONE ? 0 : eb.i);
-        msg_store(B.part + ((size_t)(T % PART_RING) * P.S + seg0 + s) * 3, msg);
+      if (!ok) {
+        grid_fail(B, TV_ETIMEOUT_DEV, SITE_WORKER_TAIL);
+        s_bad = 1;
       }
+      eb = worker_reduce_exact(eb, ered);
+      if (s_bad) return;
+      if (tid == 0) send_partial(B, P, (unsigned)T, (unsigned)T & (PART_RING - 1), seg0 + s, eb);
     }
   }
 }
 
 // ---------------------------------------------------------------------------
-// Head CTA
+// Head CTA (GRID_THREADS threads, one group of HEAD_GROUP lanes per state)
 // ---------------------------------------------------------------------------
 __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBufs& B, unsigned char* sm) {
-  const int N = m.N, D = m.D, L = P.L, S = P.S;
+  constexpr int L = GRID_L;
+  const int N = m.N, D = m.D, S = P.S;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int g = tid / HEAD_GROUP, gl = tid % HEAD_GROUP;
   const unsigned gmask = 0xffu << ((lane / HEAD_GROUP) * HEAD_GROUP);
@@ -346,22 +429,22 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   double* dur_h = (double*)(sm + P.h_dur);            // [N][L]
   long long* dq = (long long*)(sm + P.h_dq);
   long long* ptil = (long long*)(sm + P.h_ptil);
-  double* pv = (double*)(sm + P.h_pv);
+  long long* pk = (long long*)(sm + P.h_pv);          // partial winners: order keys
   int* pd = (int*)(sm + P.h_pd);
   int* pi = (int*)(sm + P.h_pi);
   double* tail = (double*)(sm + P.h_tail);
   __shared__ int s_fail;
 
-  for (int k = tid; k < N * N; k += blockDim.x) qtr[k] = m.qtr[k];
-  for (int k = tid; k < N * L; k += blockDim.x) {
+  for (int k = tid; k < N * N; k += GRID_THREADS) qtr[k] = m.qtr[k];
+  for (int k = tid; k < N * L; k += GRID_THREADS) {
     const int j = k / L, d = k % L;
     qd_h[k] = m.qdurT[(size_t)j * D + d];
     dur_h[k] = m.durT[(size_t)j * D + d];
   }
-  for (int j = tid; j < N; j += blockDim.x) {
+  for (int j = tid; j < N; j += GRID_THREADS) {
     const double d0 = B.dinit[j];
     dstar_h[j] = d0;
-    B.dstar_g[j] = d0;
+    tagged64_store(B.dstar + (size_t)j * 2, 1u, (unsigned long long)__double_as_longlong(d0));
     dq[j] = quantize(d0, m.scale);
     ptil[j] = m.qem[(size_t)B.obs[0] * N + j];
     B.psi[j] = pack_psi(0, 0);
@@ -370,25 +453,31 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   const int j = g;  // this group's state (N <= GRID_MAX_N)
   const bool has_j = j < N;
   double di_cur = 0.0;
-  if (has_j && 1 < D) di_cur = __ldcg(B.dinit + (size_t)1 * N + j);
+  if (has_j && gl == 0 && 1 < D) di_cur = __ldcg(B.dinit + (size_t)1 * N + j);
+  TaggedMsg pm;
+  if (tid < S) msg_load(B.part + ((size_t)(1 & (PART_RING - 1)) * S + tid) * 3, pm);
   __syncthreads();
 
+  int hrow = 0;        // (t-1) % L: row of slot t-1 in ctil_h / itil_h
+  int drow_prev = 0;   // (t-1) % (L+1): row of delta[t-1] in dstar_h
+  int rdrow = 1;       // t % Rd: row of delta[t] in the tagged ring
   for (long long t = 1; t < T; ++t) {
     const int tau = (int)(t < D ? t : D);
     const int hl = tau < L ? tau : L;
-    // Worker partials of this step: issue the loads first, check them after
-    // the matvec has hidden their latency.
-    TaggedMsg pm;
-    if (tid < S) msg_load(B.part + ((size_t)(t % PART_RING) * S + tid) * 3, pm);
+    const int drow = drow_prev + 1 == L + 1 ? 0 : drow_prev + 1;  // t % (L+1)
+    // Next step's partials (or the tail's) are fetched one step early.
+    TaggedMsg pm_next;
+    if (tid < S) msg_load(B.part + ((size_t)((unsigned)(t + 1) & (PART_RING - 1)) * S + tid) * 3, pm_next);
     const int ot = B.obs[t];
     double di_next = 0.0;
-    if (has_j && t + 1 < D) di_next = __ldcg(B.dinit + (size_t)(t + 1) * N + j);
+    if (has_j && gl == 0 && t + 1 < D) di_next = __ldcg(B.dinit + (size_t)(t + 1) * N + j);
 
-    // Phase B: matvec for slot s = t-1, its publication, P(t), window sums.
+    // Phase B: matvec for slot s = t-1 and its message, P(t), window sums.
     if (has_j) {
       Top2 tb;
       tb.init();
-      for (int i = gl; i < N; i += HEAD_GROUP) tb.push(qtr[j * N + i] + dq[i], i);
+      const long long* qrow = qtr + j * N;
+      for (int i = gl; i < N; i += HEAD_GROUP) tb.push(qrow[i] + dq[i], i);
 #pragma unroll
       for (int o = HEAD_GROUP / 2; o > 0; o >>= 1) {
         const long long ob1 = __shfl_xor_sync(gmask, tb.b1, o);
@@ -396,55 +485,63 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
         const int ox1 = __shfl_xor_sync(gmask, tb.x1, o);
         tb.merge(ob1, ox1, ob2);
       }
-      const double emt = m.em[(size_t)ot * N + j];
       if (t > D) {
         // E_t[d] = E_{t-1}[d-1] + em_t, E_t[0] = 0 + em_t (src/hsmm.cu:298-310)
         const double old = gl < L ? E_h[gl * N + j] : 0.0;
         const double prev = __shfl_up_sync(gmask, old, 1, HEAD_GROUP);
-        if (gl < L) E_h[gl * N + j] = (gl == 0 ? 0.0 : prev) + emt;
+        if (gl < L) {
+          const double emt = m.em[(size_t)ot * N + j];
+          if (gl == 0) {
+            long long b = __double_as_longlong(emt);
+            E_h[j] = __longlong_as_double(b == (long long)0x8000000000000000ULL ? 0 : b);  // 0 + em_t
+          } else {
+            E_h[gl * N + j] = prev + emt;
+          }
+        }
       } else if (gl == 0) {
         // newest-first rebuild (src/hsmm.cu:311-322)
-        double gsum = emt;
+        double gsum = m.em[(size_t)ot * N + j];
         E_h[j] = gsum;
         for (int d = 1; d < hl; ++d) {
           gsum = gsum + m.em[(size_t)B.obs[t - d] * N + j];
           E_h[d * N + j] = gsum;
         }
       }
-      if (gl == 0) {
-        const long long c = tb.b1 - ptil[j];
-        const bool amb = (tb.b1 - tb.b2) <= m.margin;
-        const unsigned short itv = (unsigned short)(tb.x1 | (amb ? 0x8000 : 0));
-        const int hrow = (int)((t - 1) % L);
+      unsigned long long* msg =
+          B.slot_msg + ((size_t)((unsigned)(t - 1) & (SLOT_RING - 1)) * N + j) * SLOT_WORDS;
+      const unsigned tag = (unsigned)t;  // slot t-1
+      const long long c = tb.b1 - ptil[j];
+      const bool amb = (tb.b1 - tb.b2) <= m.margin;
+      const unsigned short itv = (unsigned short)(tb.x1 | (amb ? 0x8000 : 0));
+      if (gl == 0) tagged64_store(msg, tag, (unsigned long long)c);
+      if (gl == 1)
+        tagged64_store(msg + 2, tag, (unsigned long long)__double_as_longlong(dstar_h[drow_prev * N + tb.x1]));
+      if (gl == 2) st_relaxed_u64(msg + 4, ((unsigned long long)tag << 32) | itv);
+      if (gl == 3) {
         ctil_h[hrow * N + j] = c;
         itil_h[hrow * N + j] = itv;
-        const size_t rec = (size_t)((t - 1) % SLOT_RING) * N + j;
-        B.slot_ctil[rec] = c;
-        B.slot_itil[rec] = itv;
-        B.slot_dsel[rec] = dstar_h[(size_t)((t - 1) % (L + 1)) * N + tb.x1];
-        ptil[j] += m.qem[(size_t)ot * N + j];
       }
+      if (gl == 4) ptil[j] += m.qem[(size_t)ot * N + j];
     }
     if (tid < S) {
-      if (!msg_wait(B.part + ((size_t)(t % PART_RING) * S + tid) * 3, (unsigned)t, pm, B.abort_flag, P.timeout)) {
-        grid_fail(B, TV_ETIMEOUT_DEV);
+      if (!msg_wait(B.part + ((size_t)((unsigned)t & (PART_RING - 1)) * S + tid) * 3, (unsigned)t, pm, B.abort_flag,
+                    P.timeout)) {
+        grid_fail(B, TV_ETIMEOUT_DEV, SITE_HEAD_PARTIAL);
         s_fail = 1;
       } else {
-        msg_unpack(pm, pv[tid], pd[tid], pi[tid]);
+        double v;
+        msg_unpack(pm, v, pd[tid], pi[tid]);
+        pk[tid] = order_key(v);
       }
     }
     __syncthreads();
     if (s_fail) return;
-    if (tid == 0) {
-      __threadfence();
-      st_release_u32(B.pub, (unsigned)t);  // slots 0..t-1 are published
-    }
 
     // Phase C: the head's candidates d < L, certified; merge; finalise.
     if (has_j) {
       Top2 tb;
       tb.init();
-      for (int d = gl; d < hl; d += HEAD_GROUP) tb.push(ctil_h[(int)((t - 1 - d) % L) * N + j] + qd_h[j * L + d], d);
+      if (gl < hl) tb.push(ctil_h[((hrow - gl) & (L - 1)) * N + j] + qd_h[j * L + gl], gl);
 #pragma unroll
       for (int o = HEAD_GROUP / 2; o > 0; o >>= 1) {
         const long long ob1 = __shfl_xor_sync(gmask, tb.b1, o);
@@ -453,56 +550,65 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
         tb.merge(ob1, ox1, ob2);
       }
       const int d1 = tb.x1;
-      const unsigned short it = itil_h[(int)((t - 1 - d1) % L) * N + j];
+      const unsigned short it = itil_h[((hrow - d1) & (L - 1)) * N + j];
       const bool amb = (it & 0x8000) || ((tb.b1 - tb.b2) <= m.margin);
       ExactBest eb;
       eb.init();
       if (!amb) {
-        const int i1 = it & 0x7fff;
-        eb.v = (E_h[d1 * N + j] + dstar_h[(size_t)((t - 1 - d1) % (L + 1)) * N + i1]) +
-               (m.trans[(size_t)j * N + i1] + dur_h[j * L + d1]);
-        eb.d = d1;
-        eb.i = i1;
+        if (gl == 0) {
+          const int i1 = it & 0x7fff;
+          int dr = drow_prev - d1;
+          if (dr < 0) dr += L + 1;
+          eb.set((E_h[d1 * N + j] + dstar_h[dr * N + i1]) + (m.trans[(size_t)j * N + i1] + dur_h[j * L + d1]), d1,
+                 i1);
+        }
       } else {
         const long long thr = tb.b1 - m.margin;
-        for (int d = gl; d < hl; d += HEAD_GROUP) {
-          if (ctil_h[(int)((t - 1 - d) % L) * N + j] + qd_h[j * L + d] < thr) continue;
+        if (gl < hl && ctil_h[((hrow - gl) & (L - 1)) * N + j] + qd_h[j * L + gl] >= thr) {
+          const int d = gl;
           const double e = E_h[d * N + j];
           const double du = dur_h[j * L + d];
-          const double* row = dstar_h + (size_t)((t - 1 - d) % (L + 1)) * N;
-          const double* tr = m.trans + (size_t)j * N;
-          for (int i = 0; i < N; ++i) eb.offer((e + row[i]) + (tr[i] + du), d, i);
+          int dr = drow_prev - d;
+          if (dr < 0) dr += L + 1;
+          const double* row = dstar_h + dr * N;
+          const double* trj = m.trans + (size_t)j * N;
+          for (int i = 0; i < N; ++i) eb.offer((e + row[i]) + (trj[i] + du), d, i);
         }
 #pragma unroll
         for (int o = HEAD_GROUP / 2; o > 0; o >>= 1) {
-          const double ov = __shfl_xor_sync(gmask, eb.v, o);
+          const long long ok = __shfl_xor_sync(gmask, eb.k, o);
           const int od = __shfl_xor_sync(gmask, eb.d, o);
           const int oi = __shfl_xor_sync(gmask, eb.i, o);
-          eb.offer(ov, od, oi);
+          eb.offer_key(ok, od, oi);
         }
       }
-      const int k0 = B.seg_first[j], k1 = k0 + B.seg_count[j];
-      for (int k = k0; k < k1; ++k)
-        if (pd[k] != EMPTY_D) eb.offer(pv[k], pd[k], pi[k]);
       if (gl == 0) {
+        const int k0 = B.seg_first[j], k1 = k0 + B.seg_count[j];
+        for (int k = k0; k < k1; ++k)
+          if (pd[k] != EMPTY_D) eb.offer_key(pk[k], pd[k], pi[k]);
         double fin;
         uint32_t wv;
         // t < D: the induction result replaces the initialisation score only
         // when strictly larger (src/hsmm.cu:353-358).
-        if (t >= D || eb.v > di_cur) {
-          fin = eb.v;
+        if (t >= D || eb.k > order_key(di_cur)) {
+          fin = eb.value();
           wv = pack_psi(eb.d, eb.i);
         } else {
           fin = di_cur;
           wv = pack_psi((int)t, 0);
         }
-        dstar_h[(size_t)(t % (L + 1)) * N + j] = fin;
-        B.dstar_g[(size_t)(t % P.Rd) * N + j] = fin;
+        dstar_h[drow * N + j] = fin;
+        tagged64_store(B.dstar + ((size_t)rdrow * N + j) * 2, (unsigned)(t + 1),
+                       (unsigned long long)__double_as_longlong(fin));
         dq[j] = quantize(fin, m.scale);
         B.psi[(size_t)t * N + j] = wv;
       }
     }
     di_cur = di_next;
+    pm = pm_next;
+    hrow = (hrow + 1) & (L - 1);
+    drow_prev = drow;
+    rdrow = rdrow + 1 == P.Rd ? 0 : rdrow + 1;
     __syncthreads();
   }
 
@@ -511,14 +617,15 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
     const long long t = T - 1;
     const int tau = (int)(t < D ? t : D);
     const int hl = tau < L ? tau : L;
-    TaggedMsg pm;
     if (tid < S) {
-      msg_load(B.part + ((size_t)(T % PART_RING) * S + tid) * 3, pm);
-      if (!msg_wait(B.part + ((size_t)(T % PART_RING) * S + tid) * 3, (unsigned)T, pm, B.abort_flag, P.timeout)) {
-        grid_fail(B, TV_ETIMEOUT_DEV);
+      if (!msg_wait(B.part + ((size_t)((unsigned)T & (PART_RING - 1)) * S + tid) * 3, (unsigned)T, pm, B.abort_flag,
+                    P.timeout)) {
+        grid_fail(B, TV_ETIMEOUT_DEV, SITE_HEAD_TAIL);
         s_fail = 1;
       } else {
-        msg_unpack(pm, pv[tid], pd[tid], pi[tid]);
+        double v;
+        msg_unpack(pm, v, pd[tid], pi[tid]);
+        pk[tid] = order_key(v);
       }
     }
     __syncthreads();
@@ -526,25 +633,30 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
     if (has_j) {
       ExactBest eb;
       eb.init();
-      for (int d = gl; d < hl; d += HEAD_GROUP) {
+      if (gl < hl) {
+        const int d = gl;
         const double e = E_h[d * N + j] + m.survT[(size_t)j * D + d];
-        const double* row = dstar_h + (size_t)((t - 1 - d) % (L + 1)) * N;
-        const double* tr = m.trans + (size_t)j * N;
-        for (int i = 0; i < N; ++i) eb.offer((e + row[i]) + tr[i], d, i);
+        // after the loop drow_prev is the row of delta[T-1]; the tail reads
+        // delta[t-1-d] = delta[T-2-d]
+        int dr = drow_prev - 1 - d;
+        if (dr < 0) dr += L + 1;
+        const double* row = dstar_h + dr * N;
+        const double* trj = m.trans + (size_t)j * N;
+        for (int i = 0; i < N; ++i) eb.offer((e + row[i]) + trj[i], d, i);
       }
 #pragma unroll
       for (int o = HEAD_GROUP / 2; o > 0; o >>= 1) {
-        const double ov = __shfl_xor_sync(gmask, eb.v, o);
+        const long long ok = __shfl_xor_sync(gmask, eb.k, o);
         const int od = __shfl_xor_sync(gmask, eb.d, o);
         const int oi = __shfl_xor_sync(gmask, eb.i, o);
-        eb.offer(ov, od, oi);
+        eb.offer_key(ok, od, oi);
       }
-      const int k0 = B.seg_first[j], k1 = k0 + B.seg_count[j];
-      for (int k = k0; k < k1; ++k)
-        if (pd[k] != EMPTY_D) eb.offer(pv[k], pd[k], pi[k]);
       if (gl == 0) {
+        const int k0 = B.seg_first[j], k1 = k0 + B.seg_count[j];
+        for (int k = k0; k < k1; ++k)
+          if (pd[k] != EMPTY_D) eb.offer_key(pk[k], pd[k], pi[k]);
         if (eb.d == IDX_NONE) { eb.d = 0; eb.i = 0; }
-        tail[j] = eb.v;
+        tail[j] = eb.value();
         B.psi[(size_t)t * N + j] = pack_psi(eb.d, eb.i);
       }
     }
@@ -580,10 +692,11 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
 __global__ void __launch_bounds__(GRID_THREADS, 1) grid_decode_kernel(ModelView m, GridParams P, GridBufs B) {
   extern __shared__ __align__(16) unsigned char smem[];
   if (ld_relaxed_i32(B.abort_flag)) return;  // rejected observations
-  if (blockIdx.x == 0)
+  if (blockIdx.x == 0) {
     grid_head(m, P, B, smem);
-  else
+  } else if (threadIdx.x < WORKER_THREADS) {
     grid_worker(m, P, B, smem);
+  }
 }
 
 }  // namespace tv

@@ -117,10 +117,9 @@ struct tv_model_s {
   int64_t last_launches = 0;
   int sm_count = 0;
   // grid-kernel scratch (single long sequences)
-  DevBuf<long long> slot_ctil;
-  DevBuf<unsigned short> slot_itil;
-  DevBuf<double> slot_dsel, dstar_g, dinit, ck;
-  DevBuf<unsigned long long> part;
+  DevBuf<unsigned long long> msgs;  // slot messages, partial messages, exact delta ring
+  DevBuf<double> dinit, ck;
+  DevBuf<long long> wrange;
   DevBuf<int> seg_first, seg_count, seg_base, gflags;
   int plan_key_N = -1, plan_key_D = -1, plan_key_G = -1;
   tv::GridParams plan{};
@@ -273,23 +272,49 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
 }
 
 
-// Splits the N*D window cells (state-major, ring slot minor) into equal
-// contiguous chunks, one per worker CTA; a chunk's intersection with a
+// Assigns the N*D window cells (state-major, ring slot minor) to the worker
+// CTAs.  When every state can get k >= 1 whole workers, each state's ring is
+// cut into k equal parts (one segment per worker, all tables of a worker in
+// its shared memory); otherwise the cells are cut into equal contiguous
+// chunks that may span several states.  A worker's intersection with a
 // state's row is a segment and yields one partial winner per step.
-bool plan_grid(tv_model_s* m, int G, int smem_optin, tv::GridParams& P, std::vector<int>& first,
-               std::vector<int>& count, std::vector<int>& base) {
+bool plan_grid(tv_model_s* m, int G, int smem_optin, tv::GridParams& P, std::vector<long long>& wr,
+               std::vector<int>& first, std::vector<int>& count, std::vector<int>& base) {
   const int N = m->N, D = m->D, L = tv::GRID_L;
   if (G < 2 || D <= L || N > tv::GRID_MAX_N || D > 65535) return false;
   const int Gw = G - 1;
   const long long ND = (long long)N * D;
-  const long long chunk = (ND + Gw - 1) / Gw;
+  wr.assign(2 * (size_t)Gw, 0);
+  long long chunk = 0;
+  const int k = Gw / N;
+  if (k >= 1) {
+    const int parts = (int)std::min<long long>(k, D);
+    const long long part = (D + parts - 1) / parts;
+    int w = 0;
+    for (int j = 0; j < N; ++j)
+      for (int q = 0; q < parts; ++q, ++w) {
+        const long long lo = (long long)j * D + (long long)q * part;
+        const long long hi = std::min((long long)j * D + (long long)(q + 1) * part, (long long)(j + 1) * D);
+        wr[2 * w] = lo;
+        wr[2 * w + 1] = std::max(lo, hi);
+      }
+    for (; w < Gw; ++w) wr[2 * w] = wr[2 * w + 1] = ND;
+    chunk = part;
+  } else {
+    chunk = (ND + Gw - 1) / Gw;
+    for (int w = 0; w < Gw; ++w) {
+      const long long lo = std::min((long long)w * chunk, ND), hi = std::min(lo + chunk, ND);
+      wr[2 * w] = lo;
+      wr[2 * w + 1] = hi;
+    }
+  }
   first.assign(N, 0);
   count.assign(N, 0);
   base.assign(Gw, 0);
   std::vector<int> seen(N, 0);
   int S = 0, max_seg = 0;
   for (int w = 0; w < Gw; ++w) {
-    const long long lo = (long long)w * chunk, hi = std::min(lo + chunk, ND);
+    const long long lo = wr[2 * w], hi = wr[2 * w + 1];
     base[w] = S;
     if (lo >= hi) continue;
     const int ja = (int)(lo / D), jb = (int)((hi - 1) / D);
@@ -307,11 +332,14 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, tv::GridParams& P, std::vec
   P.chunk = chunk; P.max_seg = max_seg;
   unsigned long long o = 0;
   P.w_qd = o;   o = tv::tv_align(o + (unsigned long long)max_seg * D * 8);
+  P.w_dur = o;  o = tv::tv_align(o + (unsigned long long)max_seg * D * 8);
+  P.w_tr = o;   o = tv::tv_align(o + (unsigned long long)max_seg * N * 8);
   P.w_ctil = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
   P.w_dsel = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
-  P.w_acc = o;  o = tv::tv_align(o + (unsigned long long)chunk * 8);
+  P.w_acc0 = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
+  P.w_acc1 = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
   P.w_itil = o; o = tv::tv_align(o + (unsigned long long)chunk * 2);
-  P.w_red = o;  o = tv::tv_align(o + (unsigned long long)std::max(max_seg * 32 * sizeof(tv::Top2), 32 * sizeof(tv::ExactBest)));
+  P.w_red = o;  o = tv::tv_align(o + (unsigned long long)std::max(max_seg * (tv::WORKER_THREADS / 32) * sizeof(tv::Top2), 32 * sizeof(tv::ExactBest)));
   P.w_bytes = o;
   o = 0;
   P.h_qtr = o;   o = tv::tv_align(o + (unsigned long long)N * N * 8);
@@ -323,11 +351,10 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, tv::GridParams& P, std::vec
   P.h_dur = o;   o = tv::tv_align(o + (unsigned long long)N * L * 8);
   P.h_dq = o;    o = tv::tv_align(o + (unsigned long long)N * 8);
   P.h_ptil = o;  o = tv::tv_align(o + (unsigned long long)N * 8);
-  P.h_pv = o;    o = tv::tv_align(o + (unsigned long long)S * 8);
+  P.h_pv = o;    o = tv::tv_align(o + (unsigned long long)S * 8);  // order keys
   P.h_pd = o;    o = tv::tv_align(o + (unsigned long long)S * 4);
   P.h_pi = o;    o = tv::tv_align(o + (unsigned long long)S * 4);
   P.h_tail = o;  o = tv::tv_align(o + (unsigned long long)N * 8);
-  P.h_red = o;
   P.h_bytes = o;
   P.timeout = 1LL << 31;  // SM clock cycles, about a second: no legitimate wait comes close
   return std::max(P.w_bytes, P.h_bytes) + 256 <= (unsigned long long)smem_optin;
@@ -340,16 +367,16 @@ int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_
   int rc;
   if ((rc = prepare_quant(m, Q, st)) != TV_OK) return rc;
   if ((rc = m->psi.ensure((size_t)T * N)) != TV_OK) return rc;
-  if ((rc = m->slot_ctil.ensure((size_t)tv::SLOT_RING * N)) != TV_OK) return rc;
-  if ((rc = m->slot_itil.ensure((size_t)tv::SLOT_RING * N)) != TV_OK) return rc;
-  if ((rc = m->slot_dsel.ensure((size_t)tv::SLOT_RING * N)) != TV_OK) return rc;
-  if ((rc = m->part.ensure((size_t)tv::PART_RING * P.S * 3)) != TV_OK) return rc;
-  if ((rc = m->dstar_g.ensure((size_t)P.Rd * N)) != TV_OK) return rc;
+  const size_t slot_words = (size_t)tv::SLOT_RING * N * tv::SLOT_WORDS;
+  const size_t part_words = (size_t)tv::PART_RING * P.S * 3;
+  const size_t dstar_words = (size_t)P.Rd * N * 2;
+  if ((rc = m->msgs.ensure(slot_words + part_words + dstar_words)) != TV_OK) return rc;
   if ((rc = m->dinit.ensure((size_t)D * N)) != TV_OK) return rc;
   const int tmax = (int)std::min<int64_t>(D, T - 1);
   if ((rc = m->ck.ensure((size_t)std::max(tmax, 1) * P.M * N)) != TV_OK) return rc;
   if ((rc = m->gflags.ensure(4)) != TV_OK) return rc;
-  TV_CUDA(cudaMemsetAsync(m->part.p, 0, sizeof(unsigned long long) * tv::PART_RING * P.S * 3, st));
+  // Tags start at 1: a cleared buffer holds no valid message.
+  TV_CUDA(cudaMemsetAsync(m->msgs.p, 0, sizeof(unsigned long long) * (slot_words + part_words + dstar_words), st));
   TV_CUDA(cudaMemsetAsync(m->gflags.p, 0, sizeof(int) * 4, st));
   tv::ModelView mv = view(m, Q);
   int* gabort = m->gflags.p + 1;
@@ -369,19 +396,18 @@ int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_
   B.psi = m->psi.p;
   B.path = path_dev;
   B.loglik = ll_dev;
-  B.slot_ctil = m->slot_ctil.p;
-  B.slot_itil = m->slot_itil.p;
-  B.slot_dsel = m->slot_dsel.p;
-  B.part = m->part.p;
-  B.dstar_g = m->dstar_g.p;
+  B.slot_msg = m->msgs.p;
+  B.part = m->msgs.p + slot_words;
+  B.dstar = m->msgs.p + slot_words + part_words;
   B.dinit = m->dinit.p;
   B.ck = m->ck.p;
+  B.wrange = m->wrange.p;
   B.seg_first = m->seg_first.p;
   B.seg_count = m->seg_count.p;
   B.seg_base = m->seg_base.p;
-  B.pub = (unsigned*)(m->gflags.p + 0);
-  B.abort_flag = m->gflags.p + 1;
-  B.status = m->gflags.p + 2;
+  B.abort_flag = gabort;
+  B.status = gstatus;
+  B.site = m->gflags.p + 0;
   tv::GridParams Pc = P;
   void* args[] = {&mv, &Pc, &B};
   const size_t dyn = std::max(P.w_bytes, P.h_bytes);
@@ -413,10 +439,11 @@ int launch_single(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* pat
     if (m->grid_ctas > 0) G = std::min(G, m->grid_ctas);
     if (m->plan_key_N != m->N || m->plan_key_D != m->D || m->plan_key_G != G) {
       std::vector<int> first, count, base;
+      std::vector<long long> wr;
       tv::GridParams P;
-      if (!plan_grid(m, G, smem_optin, P, first, count, base)) {
+      if (!plan_grid(m, G, smem_optin, P, wr, first, count, base)) {
         if (m->path_pref == TV_PATH_GRID)
-          return fail(TV_EINVAL, "the grid kernel cannot take this shape (needs D > 4, N <= 128, D <= 65535)");
+          return fail(TV_EINVAL, "the grid kernel cannot take this shape (needs D > 8, N <= 128, D <= 65535, and the per-CTA share of the window in shared memory)");
         want = TV_PATH_CTA;
       } else {
         const size_t dyn = std::max(P.w_bytes, P.h_bytes);
@@ -427,6 +454,8 @@ int launch_single(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* pat
         if ((rc = m->seg_first.ensure(first.size())) != TV_OK) return rc;
         if ((rc = m->seg_count.ensure(count.size())) != TV_OK) return rc;
         if ((rc = m->seg_base.ensure(base.size())) != TV_OK) return rc;
+        if ((rc = m->wrange.ensure(wr.size())) != TV_OK) return rc;
+        TV_CUDA(cudaMemcpy(m->wrange.p, wr.data(), sizeof(long long) * wr.size(), cudaMemcpyHostToDevice));
         TV_CUDA(cudaMemcpy(m->seg_first.p, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice));
         TV_CUDA(cudaMemcpy(m->seg_count.p, count.data(), sizeof(int) * count.size(), cudaMemcpyHostToDevice));
         TV_CUDA(cudaMemcpy(m->seg_base.p, base.data(), sizeof(int) * base.size(), cudaMemcpyHostToDevice));
@@ -450,7 +479,13 @@ int read_grid_status(tv_model_s* m, cudaStream_t st) {
   int s[4] = {0, 0, 0, 0};
   TV_CUDA(cudaMemcpyAsync(s, m->gflags.p, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
   TV_CUDA(cudaStreamSynchronize(st));
-  if (s[2] == tv::TV_ETIMEOUT_DEV) return fail(TV_ETIMEOUT, "grid decode: a bounded wait between CTAs timed out");
+  if (s[2] == tv::TV_ETIMEOUT_DEV) {
+    static const char* sites[] = {"?", "head waiting for worker partials", "worker waiting for a slot message",
+                                  "worker re-scoring waiting for an exact score", "worker tail waiting for an exact score",
+                                  "head waiting for tail partials"};
+    const int k = (s[0] >= 1 && s[0] <= 5) ? s[0] : 0;
+    return fail(TV_ETIMEOUT, std::string("grid decode: a bounded wait between CTAs timed out (") + sites[k] + ")");
+  }
   if (s[2] == TV_ERANGE) return fail(TV_ERANGE, "an observation is outside [0, O)");
   if (s[2] != 0) return fail(TV_EINTERNAL, "grid decode: device back-pointer check failed");
   return TV_OK;
@@ -526,8 +561,7 @@ int tv_model_destroy(tv_model m) {
   m->em.release(); m->trans.release(); m->start.release(); m->durT.release(); m->survT.release();
   m->qem.release(); m->qtr.release(); m->qdurT.release();
   m->psi.release(); m->status.release(); m->counter.release(); m->off.release(); m->scratch.release();
-  m->slot_ctil.release(); m->slot_itil.release(); m->slot_dsel.release(); m->dstar_g.release();
-  m->dinit.release(); m->ck.release(); m->part.release();
+  m->msgs.release(); m->dinit.release(); m->ck.release(); m->wrange.release();
   m->seg_first.release(); m->seg_count.release(); m->seg_base.release(); m->gflags.release();
   if (m->ev0) cudaEventDestroy(m->ev0);
   if (m->ev1) cudaEventDestroy(m->ev1);

@@ -84,6 +84,32 @@ __device__ __forceinline__ bool msg_wait(const unsigned long long* src, unsigned
   }
 }
 
+// A 64-bit payload sent as two tagged words (low half, high half).
+__device__ __forceinline__ void tagged64_store(unsigned long long* dst, unsigned tag, unsigned long long payload) {
+  const unsigned long long hi = (unsigned long long)tag << 32;
+  st_relaxed_u64(dst + 0, hi | (payload & 0xffffffffull));
+  st_relaxed_u64(dst + 1, hi | (payload >> 32));
+}
+
+// Loads a tagged 64-bit payload, polling until both halves carry `tag`.
+__device__ __forceinline__ bool tagged64_load(const unsigned long long* src, unsigned tag, unsigned long long& payload,
+                                              const int* abort_flag, long long limit) {
+  unsigned long long a = ld_relaxed_u64(src), b = ld_relaxed_u64(src + 1);
+  if ((unsigned)(a >> 32) != tag || (unsigned)(b >> 32) != tag) {
+    const long long t0 = clock64();
+    for (;;) {
+      __nanosleep(20);
+      a = ld_relaxed_u64(src);
+      b = ld_relaxed_u64(src + 1);
+      if ((unsigned)(a >> 32) == tag && (unsigned)(b >> 32) == tag) break;
+      if (ld_relaxed_i32(abort_flag)) return false;
+      if (clock64() - t0 > limit) return false;
+    }
+  }
+  payload = (a & 0xffffffffull) | ((b & 0xffffffffull) << 32);
+  return true;
+}
+
 // Poll a monotonic counter until it reaches `target`.
 __device__ __forceinline__ bool wait_geq(const unsigned* p, unsigned target, unsigned& seen, const int* abort_flag,
                                          long long limit) {

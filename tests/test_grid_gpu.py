@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _grid_ok(N, D):
-    return D > 4 and N <= 128
+    return D > 8 and N <= 128
 
 
 @pytest.mark.parametrize("grid_ctas", [0, 5])
@@ -21,7 +21,7 @@ def test_grid_golden(tvlib, name, grid_ctas):
     args, z = load_golden(name)
     N, D = args[0], args[5].shape[0]
     if not _grid_ok(N, D):
-        pytest.skip("shape outside the grid kernel (D <= 4)")
+        pytest.skip("shape outside the grid kernel (D <= 8)")
     ref = orc.decode(*args)
     with tvlib.Model(*args[:6]) as m:
         m.set_path("grid", grid_ctas)
@@ -44,7 +44,7 @@ def test_grid_random_vs_oracle_and_cta(tvlib, seed):
     p = syn.discrete_problem(N, D, T, M, lo, hi, seed=seed)
     ref = orc.decode(*p.args(), variant="omp")
     with tvlib.Model(*p.model_args()) as m:
-        m.set_path("grid", int(rng.integers(2, 40)))
+        m.set_path("grid", int(rng.integers(N // 2 + 2, 160)))
         pg, lg = m.decode(p.obs_seq, return_loglik=True)
         m.set_path("cta")
         pc, lc = m.decode(p.obs_seq, return_loglik=True)
