@@ -122,6 +122,35 @@ int tv_model_last_path(tv_model m);
 int tv_model_set_timing(tv_model m, int enable);
 double tv_model_kernel_ms(tv_model m);
 
+/*
+ * Decode one sequence without allocating device memory (no counterpart in the
+ * reference).  For callers that must not call cudaMalloc at decode time:
+ * code running inside a CUDA graph capture or a stream callback, real-time
+ * or latency-critical loops where an allocation can stall on the driver, and
+ * processes whose device memory is fully reserved up front by a pool.  The
+ * model (tv_model_create) is the only allocation, made once at set-up.
+ *
+ * Scratch (the fixed-point tables for this decode, the back-pointers and a
+ * few control words) comes from one fixed array compiled into the library,
+ * TV_STATIC_SCRATCH_BYTES large, that every GPU using the library holds until
+ * the process exits.  Limits: 8*(O*N + N*N + N*D) + 4*T*N + 256 bytes must fit
+ * in it, and the D-deep window must fit one CTA's shared memory
+ * (34*N*D + 8*N*N bytes <= 227 KB); larger problems return TV_ETOOBIG.
+ *
+ * The first call on a device looks the array up (cudaGetSymbolAddress) and
+ * sets the kernel's shared-memory attribute with that device current; make
+ * that first call before any stream capture.  All calls share the one array
+ * and leave their data in it: calls that overlap on the GPU (other streams,
+ * other threads, other models) race; serialise them.  obs_dev, path_dev
+ * (T int32), loglik_dev (1 double) and status_dev (1 int, 0 on success, or a
+ * TV_* code such as TV_ERANGE for an observation outside [0, O)) are device
+ * pointers; loglik_dev and status_dev may be NULL.  Asynchronous on `stream`.
+ */
+#define TV_STATIC_SCRATCH_BYTES (32u << 20)
+int tv_decode_device_static(tv_model m, const int32_t* obs_dev, int64_t T,
+                            int32_t* path_dev, double* loglik_dev, int* status_dev,
+                            void* stream);
+
 #ifdef __cplusplus
 }
 #endif

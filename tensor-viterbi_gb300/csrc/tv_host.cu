@@ -504,6 +504,55 @@ int read_status(tv_model_s* m, int n_seq, cudaStream_t st) {
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Fixed-scratch decode (tv_decode_device_static): the one-CTA kernel with all
+// of its global scratch carved out of this file-scope array, so the call
+// allocates nothing.  Host code must not use the array's name as an address
+// (it is a host-side stand-in); the device address is looked up once per
+// device with cudaGetSymbolAddress.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_static_scratch[TV_STATIC_SCRATCH_BYTES];
+
+namespace {
+
+std::mutex g_static_mu;
+constexpr int kMaxDevices = 64;
+unsigned char* g_static_ptr[kMaxDevices] = {};
+
+// Start-of-call reset of the control words this call relies on: the work
+// queue counter and the status must start at zero (the array keeps whatever
+// the previous call left).
+__global__ void static_reset_kernel(int64_t* off, long long T, int* counter, int* status) {
+  off[0] = 0;
+  off[1] = T;
+  *counter = 0;
+  *status = 0;
+}
+
+__global__ void static_status_kernel(const int* status, int* out) { *out = *status; }
+
+int static_scratch_for_current_device(unsigned char** out) {
+  int dev = 0;
+  TV_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(TV_EINVAL, "device ordinal out of range");
+  std::lock_guard<std::mutex> lk(g_static_mu);
+  if (!g_static_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(TV_ECUDA, std::string("cudaGetSymbolAddress(static scratch): ") + cudaGetErrorString(e));
+    int smem_optin = 0;
+    TV_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    TV_CUDA(cudaFuncSetAttribute(tv::cta_decode_kernel<kThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem_optin - 64));
+    g_static_ptr[dev] = (unsigned char*)p;
+  }
+  *out = g_static_ptr[dev];
+  return TV_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* tv_last_error(void) { return g_err.c_str(); }
@@ -679,6 +728,72 @@ int tv_decode_tensor_viterbi_cuda(int n_states, int n_symbols, int max_dur, int6
   tv_model_destroy(m);
   g_err = keep;
   return rc;
+}
+
+
+int tv_decode_device_static(tv_model m, const int32_t* obs_dev, int64_t T, int32_t* path_dev, double* ll_dev,
+                            int* status_dev, void* stream) {
+  if (!m || !obs_dev || !path_dev) return fail(TV_EINVAL, "null argument");
+  if (T <= 0 || T > 0x7fffffffLL) return fail(TV_ETOOBIG, "T must be in [1, 2^31-1]");
+  const int N = m->N, O = m->O, D = m->D;
+  if (T < D)
+    return fail(TV_ESHORT, "T=" + std::to_string(T) + " < D=" + std::to_string(D) +
+                               "; the reference initialisation needs T >= D");
+  // Carve the scratch: quantised tables, offsets + control words, back-pointers.
+  auto al = [](unsigned long long x) { return (x + 255ull) & ~255ull; };
+  const unsigned long long o_qem = 0;
+  const unsigned long long o_qtr = al(o_qem + 8ull * O * N);
+  const unsigned long long o_qd = al(o_qtr + 8ull * N * N);
+  const unsigned long long o_ctl = al(o_qd + 8ull * N * D);
+  const unsigned long long o_psi = al(o_ctl + 64);
+  const unsigned long long need = o_psi + 4ull * (unsigned long long)T * N;
+  if (need > TV_STATIC_SCRATCH_BYTES)
+    return fail(TV_ETOOBIG, "problem needs " + std::to_string(need) + " bytes of scratch; the fixed-scratch entry "
+                            "point has " + std::to_string((unsigned long long)TV_STATIC_SCRATCH_BYTES) +
+                            " (use tv_decode_device)");
+  int dev = 0;
+  TV_CUDA(cudaGetDevice(&dev));
+  int smem_optin = 0;
+  TV_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  tv::CtaLayout L = tv::make_cta_layout(N, D);
+  if (L.bytes + 64 > (unsigned long long)smem_optin)
+    return fail(TV_ETOOBIG, "the D-deep window does not fit one CTA's shared memory; the fixed-scratch entry "
+                            "point decodes windows up to 34*N*D + 8*N*N = " + std::to_string(smem_optin - 64) +
+                            " bytes (use tv_decode_device)");
+  L.in_smem = 1;
+  unsigned char* base = nullptr;
+  int rc = static_scratch_for_current_device(&base);
+  if (rc != TV_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  long long* qem = (long long*)(base + o_qem);
+  long long* qtr = (long long*)(base + o_qtr);
+  long long* qd = (long long*)(base + o_qd);
+  int64_t* off = (int64_t*)(base + o_ctl);
+  int* counter = (int*)(base + o_ctl + 16);
+  int* status = (int*)(base + o_ctl + 20);
+  uint32_t* psi = (uint32_t*)(base + o_psi);
+  const Quant Q = choose_quant(m, T);
+  static_reset_kernel<<<1, 1, 0, st>>>(off, T, counter, status);
+  quantize_kernel<<<64, 256, 0, st>>>(m->em.p, qem, (size_t)O * N, Q.scale);
+  quantize_kernel<<<64, 256, 0, st>>>(m->trans.p, qtr, (size_t)N * N, Q.scale);
+  quantize_kernel<<<64, 256, 0, st>>>(m->durT.p, qd, (size_t)N * D, Q.scale);
+  tv::ModelView v = view(m, Q);
+  v.qem = qem;
+  v.qtr = qtr;
+  v.qdurT = qd;
+  tv::BatchView bv;
+  bv.obs = obs_dev;
+  bv.off = off;
+  bv.path = path_dev;
+  bv.loglik = ll_dev;
+  bv.psi = psi;
+  bv.status = status;
+  bv.next = counter;
+  bv.n_seq = 1;
+  tv::cta_decode_kernel<kThreads><<<1, kThreads, L.bytes, st>>>(v, bv, L, nullptr);
+  if (status_dev) static_status_kernel<<<1, 1, 0, st>>>(status, status_dev);
+  TV_CUDA(cudaGetLastError());
+  return TV_OK;
 }
 
 }  // extern "C"

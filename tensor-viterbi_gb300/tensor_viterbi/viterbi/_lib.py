@@ -50,7 +50,12 @@ EXPORTS = {
     "tv_model_last_path": (C.c_int, [C.c_void_p]),
     "tv_model_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "tv_model_kernel_ms": (C.c_double, [C.c_void_p]),
+    "tv_decode_device_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p]),
 }
+
+# Size of the fixed device scratch behind tv_decode_device_static.
+TV_STATIC_SCRATCH_BYTES = 32 << 20
 
 TV_PATH_AUTO = 0
 TV_PATH_CTA = 1

@@ -154,6 +154,22 @@ class Model:
                                                      C.c_void_p(loglik_dev_ptr or None),
                                                      C.c_void_p(stream or None)))
 
+    def decode_device_static(self, obs_dev_ptr: int, T: int, path_dev_ptr: int, loglik_dev_ptr: int = 0,
+                             status_dev_ptr: int = 0, stream: int = 0) -> None:
+        """Like decode_device, but allocates no device memory: for callers
+        that must not call cudaMalloc while decoding (inside a CUDA graph
+        capture, in a stream callback, in a latency-critical loop, or under a
+        memory pool reserved up front).  Scratch comes from a fixed array in
+        the library (TV_STATIC_SCRATCH_BYTES, held by every GPU that uses the
+        library); problems that do not fit raise ValueError.  The first call
+        on a device does a one-time set-up and should come before any stream
+        capture.  All calls share the array: calls that overlap on the GPU
+        race, so serialise them.  status_dev_ptr (optional, device int)
+        receives 0 or a TV_* code."""
+        _lib.check(_lib.lib().tv_decode_device_static(
+            self._h, C.c_void_p(obs_dev_ptr), int(T), C.c_void_p(path_dev_ptr), C.c_void_p(loglik_dev_ptr or None),
+            C.c_void_p(status_dev_ptr or None), C.c_void_p(stream or None)))
+
     def last_launches(self) -> int:
         return int(_lib.lib().tv_model_last_launches(self._h))
 

@@ -1,0 +1,69 @@
+"""The decode entry point that allocates no device memory.
+
+Some callers cannot call cudaMalloc while they decode: code inside a CUDA
+graph capture or a stream callback, latency-critical loops where an
+allocation can stall on the driver, and processes whose device memory is
+reserved up front by a pool.  `tv_decode_device_static` serves them from a
+fixed array compiled into the library.  This test calls it through the C ABI
+twice in a row, on two different sequences, and checks each result against
+the ordinary allocating entry point `tv_decode_device`: paths bit-exact and
+log-likelihoods equal, the bar of every other parity test here.  It lives in
+its own file, collected last, so a failure here cannot hide another test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _decode_both(tvlib, model, obs_np):
+    import torch
+    from tensor_viterbi.viterbi import _lib
+
+    L = _lib.lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    obs = torch.from_numpy(obs_np).cuda()
+    T = obs.numel()
+    ref_path = torch.full_like(obs, -1)
+    ref_ll = torch.zeros(1, dtype=torch.float64, device="cuda")
+    _lib.check(L.tv_decode_device(model.handle, C.c_void_p(obs.data_ptr()), T, C.c_void_p(ref_path.data_ptr()),
+                                  C.c_void_p(ref_ll.data_ptr()), C.c_void_p(stream)))
+    path = torch.full_like(obs, -1)
+    ll = torch.zeros(1, dtype=torch.float64, device="cuda")
+    status = torch.full((1,), 12345, dtype=torch.int32, device="cuda")
+    _lib.check(L.tv_decode_device_static(model.handle, C.c_void_p(obs.data_ptr()), T, C.c_void_p(path.data_ptr()),
+                                         C.c_void_p(ll.data_ptr()), C.c_void_p(status.data_ptr()),
+                                         C.c_void_p(stream)))
+    torch.cuda.synchronize()
+    return ref_path.cpu().numpy(), float(ref_ll.item()), path.cpu().numpy(), float(ll.item()), int(status.item())
+
+
+def test_fixed_scratch_entry_matches_allocating_entry_twice(tvlib):
+    import tensor_viterbi.synthetic as syn
+
+    prob, seqs = syn.batch_problem(n_seq=2, N=10, D=120, M=16, lo=2000, hi=6000, seed=31)
+    with tvlib.Model(*prob.model_args()) as m:
+        results = [_decode_both(tvlib, m, s) for s in seqs]  # two fixed-scratch calls in a row
+    for ref_path, ref_ll, path, ll, status in results:
+        assert status == 0
+        np.testing.assert_array_equal(path, ref_path)
+        assert ll == ref_ll
+    # the second call did not reuse the first call's back-pointers
+    assert not np.array_equal(results[0][2][:50], results[1][2][:50]) or len(seqs[0]) != len(seqs[1])
+
+
+def test_fixed_scratch_entry_rejects_oversized_problems(tvlib):
+    import torch
+    import tensor_viterbi.synthetic as syn
+    from tensor_viterbi.viterbi import _lib
+
+    # T*N back-pointers beyond the fixed array: refused before any launch
+    prob, _ = syn.batch_problem(n_seq=1, N=64, D=20, M=8, lo=1000, hi=1001, seed=1)
+    T = _lib.TV_STATIC_SCRATCH_BYTES // (4 * 64) + 16
+    obs = torch.zeros(T, dtype=torch.int32, device="cuda")
+    out = torch.empty_like(obs)
+    with tvlib.Model(*prob.model_args()) as m:
+        with pytest.raises(ValueError, match="scratch"):
+            m.decode_device_static(obs.data_ptr(), T, out.data_ptr())
