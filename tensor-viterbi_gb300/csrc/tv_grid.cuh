@@ -31,6 +31,8 @@
 // from a checkpoint table g_t(k*K) built before the launch plus at most K-1
 // additions.
 #pragma once
+#include <climits>
+
 #include "tv_cta.cuh"
 #include "tv_device.cuh"
 #include "tv_sync.cuh"
@@ -44,8 +46,10 @@ constexpr int CK_STRIDE = 32;      // checkpoint stride of the early window sums
 constexpr int PART_RING = 32;      // steps of worker partials in flight
 constexpr int SLOT_RING = 64;      // slot messages kept
 constexpr int SLOT_WORDS = 5;      // ctil (2), dsel (2), itil (1)
-constexpr int HEAD_GROUP = 8;      // lanes per state in the head
-constexpr int GRID_MAX_N = GRID_THREADS / HEAD_GROUP;
+constexpr int HEAD_GROUP = 4;      // lanes per state in the head (critical and helper warps)
+constexpr int GRID_MAX_N = 128;    // packed coarse scores keep the state index in 7 bits
+constexpr int COARSE_F = 14;       // fraction bits of the packed coarse matvec scores
+constexpr int COARSE_CLAMP = (1 << 23) - 1;
 constexpr int EMPTY_D = 0xffff;
 constexpr int TV_ETIMEOUT_DEV = -10;
 
@@ -54,8 +58,13 @@ struct GridParams {
   long long chunk;  // largest worker range, in cells
   int max_seg;
   unsigned long long w_qd, w_dur, w_tr, w_ctil, w_dsel, w_acc0, w_acc1, w_itil, w_red, w_bytes;
-  unsigned long long h_qtr, h_ctil, h_itil, h_dstar, h_E, h_qd, h_dur, h_dq, h_ptil, h_pv, h_pd, h_pi, h_tail,
-      h_bytes;
+  // head shared-memory offsets
+  unsigned long long h_qcp, h_qtr, h_dqcp, h_dq, h_ptil, h_base, h_dstar, h_ctil, h_itil, h_E, h_qd, h_dur, h_prek,
+      h_pred, h_prei, h_pwk, h_pwd, h_pwi, h_psirec, h_tail, h_bytes;
+  int Np;             // N rounded up to 16 (packed coarse matvec rows)
+  int cs_threads;     // critical-section threads (4 lanes per state, whole warps)
+  int coarse_shift;   // fine-to-coarse right shift (f - COARSE_F)
+  int coarse_margin;  // certified coarse i-margin, coarse units
   long long timeout;
 };
 
@@ -411,205 +420,385 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
 }
 
 // ---------------------------------------------------------------------------
-// Head CTA (GRID_THREADS threads, one group of HEAD_GROUP lanes per state)
+// Head CTA
+//
+// The serial critical path of a step is: the scores delta[t-1] are final ->
+// B[t-1][j] = max_i(trans[j][i] + delta[t-1][i]) for every j -> the d = 0
+// candidate -> merge with everything else -> delta[t].  Only that chain runs
+// in the critical warps (4 lanes per state, the first cs_threads threads):
+//   * the matvec in packed int32: coarse score << 7 | (127 - i), so one
+//     integer max yields the value and the lowest index; its runner-up gap is
+//     certified against a coarse margin, else a fine int64 pass decides;
+//   * the exact d = 0 score (one lane), an integer-key merge with the step's
+//     pre-merged best over d >= 1 and the init rule, quantisation.
+// The helper warps (the rest of the CTA) prepare step t+1 meanwhile: worker
+// partials, window sums, the candidates d = 1..L-1 (which need only slots
+// <= t-1), and all global stores.  A named barrier hands the matvec result
+// (slot t-1) from the critical warps to the helpers inside the step.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ void cs_arrive() {
+  asm volatile("bar.arrive 2, %0;" ::"r"(GRID_THREADS) : "memory");
+}
+__device__ __forceinline__ void helper_wait_cs() {
+  asm volatile("bar.sync 2, %0;" ::"r"(GRID_THREADS) : "memory");
+}
+
+__device__ __forceinline__ int coarse_of(long long fine_minus_base, int sh) {
+  long long v = fine_minus_base >> sh;  // arithmetic shift: floor
+  v = v > COARSE_CLAMP ? COARSE_CLAMP : (v < -COARSE_CLAMP ? -COARSE_CLAMP : v);
+  return (int)v;
+}
+
+// Packed coarse top-2: one max keeps the value and the lowest index.
+__device__ __forceinline__ void packed_push(int p, int& b1, int& b2) {
+  const int lo = min(b1, p);
+  b1 = max(b1, p);
+  b2 = max(b2, lo);
+}
+
 __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBufs& B, unsigned char* sm) {
   constexpr int L = GRID_L;
-  const int N = m.N, D = m.D, S = P.S;
+  constexpr int G4 = HEAD_GROUP;
+  const int N = m.N, D = m.D, S = P.S, Np = P.Np;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int g = tid / HEAD_GROUP, gl = tid % HEAD_GROUP;
-  const unsigned gmask = 0xffu << ((lane / HEAD_GROUP) * HEAD_GROUP);
+  const unsigned gmask = 0xfu << ((lane / G4) * G4);
   const long long T = B.T;
-  long long* qtr = (long long*)(sm + P.h_qtr);        // [N][N]
+  int* Qcp = (int*)(sm + P.h_qcp);                    // [N][Np] packed coarse trans
+  long long* qtr = (long long*)(sm + P.h_qtr);        // [N][N] fine trans
+  int* dqcp = (int*)(sm + P.h_dqcp);                  // [2][Np] packed coarse delta
+  long long* dq = (long long*)(sm + P.h_dq);          // [2][N] fine delta
+  long long* ptil = (long long*)(sm + P.h_ptil);      // [2][N] emission prefix P(t)
+  long long* basebuf = (long long*)(sm + P.h_base);   // [2] coarse base per step
+  double* dstar_h = (double*)(sm + P.h_dstar);        // [L+1][N] exact delta
   long long* ctil_h = (long long*)(sm + P.h_ctil);    // [L][N]
   unsigned short* itil_h = (unsigned short*)(sm + P.h_itil);
-  double* dstar_h = (double*)(sm + P.h_dstar);        // [L+1][N]
-  double* E_h = (double*)(sm + P.h_E);                // [L][N]
+  double* E = (double*)(sm + P.h_E);                  // [2][L][N] window sums of a step
   long long* qd_h = (long long*)(sm + P.h_qd);        // [N][L]
   double* dur_h = (double*)(sm + P.h_dur);            // [N][L]
-  long long* dq = (long long*)(sm + P.h_dq);
-  long long* ptil = (long long*)(sm + P.h_ptil);
-  long long* pk = (long long*)(sm + P.h_pv);          // partial winners: order keys
-  int* pd = (int*)(sm + P.h_pd);
-  int* pi = (int*)(sm + P.h_pi);
+  long long* prek = (long long*)(sm + P.h_prek);      // [2][N] best over d >= 1: order key
+  int* pred = (int*)(sm + P.h_pred);
+  int* prei = (int*)(sm + P.h_prei);
+  long long* pwk = (long long*)(sm + P.h_pwk);        // [S] worker partials of the next step
+  int* pwd = (int*)(sm + P.h_pwd);
+  int* pwi = (int*)(sm + P.h_pwi);
+  uint32_t* psirec = (uint32_t*)(sm + P.h_psirec);    // [2][N] back-pointer word of a step
   double* tail = (double*)(sm + P.h_tail);
   __shared__ int s_fail;
+  const int sh = P.coarse_shift;
+  const bool is_cs = tid < P.cs_threads;
+  const int hb = is_cs ? tid : tid - P.cs_threads;    // index within the role
+  const int gj = hb / G4, gl = hb % G4;                // state and lane of this group
+  const bool has_j = gj < N;
+  const int j = gj;
 
+  // ---- initial state (t = 0) ----
+  for (int k = tid; k < N * Np; k += GRID_THREADS) {
+    const int jj = k / Np, i = k % Np;
+    if (i < N) {
+      const int c = coarse_of(m.qtr[(size_t)jj * N + i], sh);
+      Qcp[k] = c * 128 + (127 - i);
+    } else {
+      Qcp[k] = INT_MIN;
+    }
+  }
   for (int k = tid; k < N * N; k += GRID_THREADS) qtr[k] = m.qtr[k];
   for (int k = tid; k < N * L; k += GRID_THREADS) {
-    const int j = k / L, d = k % L;
-    qd_h[k] = m.qdurT[(size_t)j * D + d];
-    dur_h[k] = m.durT[(size_t)j * D + d];
+    const int jj = k / L, d = k % L;
+    qd_h[k] = m.qdurT[(size_t)jj * D + d];
+    dur_h[k] = m.durT[(size_t)jj * D + d];
   }
-  for (int j = tid; j < N; j += GRID_THREADS) {
-    const double d0 = B.dinit[j];
-    dstar_h[j] = d0;
-    tagged64_store(B.dstar + (size_t)j * 2, 1u, (unsigned long long)__double_as_longlong(d0));
-    dq[j] = quantize(d0, m.scale);
-    ptil[j] = m.qem[(size_t)B.obs[0] * N + j];
-    B.psi[j] = pack_psi(0, 0);
+  for (int k = tid; k < 2 * Np; k += GRID_THREADS) dqcp[k] = 0;
+  for (int jj = tid; jj < N; jj += GRID_THREADS) {
+    const double d0 = B.dinit[jj];
+    dstar_h[jj] = d0;
+    tagged64_store(B.dstar + (size_t)jj * 2, 1u, (unsigned long long)__double_as_longlong(d0));
+    dq[jj] = quantize(d0, m.scale);
+    ptil[jj] = m.qem[(size_t)B.obs[0] * N + jj];  // P(0)
+    B.psi[jj] = pack_psi(0, 0);
+    if (T > 1) E[(1 & 1) * L * N + jj] = m.em[(size_t)B.obs[1] * N + jj];  // E_1[0]
   }
   if (tid == 0) s_fail = 0;
-  const int j = g;  // this group's state (N <= GRID_MAX_N)
-  const bool has_j = j < N;
+  __syncthreads();
+  if (warp == 0) {
+    long long mx = LLONG_MIN;
+    for (int jj = lane; jj < N; jj += 32) mx = max(mx, dq[jj]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) { basebuf[0] = mx; basebuf[1] = mx; }
+  }
+  __syncthreads();
+  for (int jj = tid; jj < N; jj += GRID_THREADS) dqcp[jj] = coarse_of(dq[jj] - basebuf[0], sh) * 128;
+  // pre-merged best over d >= 1 for step 1: only the workers' (empty) partials
+  if (tid < S) {
+    TaggedMsg pm;
+    msg_load(B.part + ((size_t)(1 & (PART_RING - 1)) * S + tid) * 3, pm);
+    if (T > 1 && !msg_wait(B.part + ((size_t)(1 & (PART_RING - 1)) * S + tid) * 3, 1u, pm, B.abort_flag, P.timeout)) {
+      grid_fail(B, TV_ETIMEOUT_DEV, SITE_HEAD_PARTIAL);
+      s_fail = 1;
+    } else {
+      double v;
+      msg_unpack(pm, v, pwd[tid], pwi[tid]);
+      pwk[tid] = order_key(v);
+    }
+  }
+  __syncthreads();
+  if (s_fail) return;
+  for (int jj = tid; jj < N; jj += GRID_THREADS) {
+    ExactBest eb;
+    eb.init();
+    const int k0 = B.seg_first[jj], k1 = k0 + B.seg_count[jj];
+    for (int k = k0; k < k1; ++k)
+      if (pwd[k] != EMPTY_D) eb.offer_key(pwk[k], pwd[k], pwi[k]);
+    prek[(1 & 1) * N + jj] = eb.k;
+    pred[(1 & 1) * N + jj] = eb.d;
+    prei[(1 & 1) * N + jj] = eb.i;
+  }
   double di_cur = 0.0;
-  if (has_j && gl == 0 && 1 < D) di_cur = __ldcg(B.dinit + (size_t)1 * N + j);
-  TaggedMsg pm;
-  if (tid < S) msg_load(B.part + ((size_t)(1 & (PART_RING - 1)) * S + tid) * 3, pm);
+  if (is_cs && has_j && gl == 0 && 1 < D) di_cur = __ldcg(B.dinit + (size_t)1 * N + j);
   __syncthreads();
 
-  int hrow = 0;        // (t-1) % L: row of slot t-1 in ctil_h / itil_h
-  int drow_prev = 0;   // (t-1) % (L+1): row of delta[t-1] in dstar_h
-  int rdrow = 1;       // t % Rd: row of delta[t] in the tagged ring
+  int drow_prev = 0;  // (t-1) % (L+1): row of delta[t-1] in dstar_h
+  int rdrow = 1;      // t % Rd: row of delta[t] in the tagged ring
   for (long long t = 1; t < T; ++t) {
-    const int tau = (int)(t < D ? t : D);
-    const int hl = tau < L ? tau : L;
+    const int cur = (int)(t & 1), prv = cur ^ 1;
     const int drow = drow_prev + 1 == L + 1 ? 0 : drow_prev + 1;  // t % (L+1)
-    // Next step's partials (or the tail's) are fetched one step early.
-    TaggedMsg pm_next;
-    if (tid < S) msg_load(B.part + ((size_t)((unsigned)(t + 1) & (PART_RING - 1)) * S + tid) * 3, pm_next);
-    const int ot = B.obs[t];
-    double di_next = 0.0;
-    if (has_j && gl == 0 && t + 1 < D) di_next = __ldcg(B.dinit + (size_t)(t + 1) * N + j);
-
-    // Phase B: matvec for slot s = t-1 and its message, P(t), window sums.
-    if (has_j) {
-      Top2 tb;
-      tb.init();
-      const long long* qrow = qtr + j * N;
-      for (int i = gl; i < N; i += HEAD_GROUP) tb.push(qrow[i] + dq[i], i);
+    const int hrow = (int)((t - 1) & (L - 1));                      // slot t-1 in ctil_h
+    if (is_cs) {
+      // ================= critical warps =================
+      double di_next = 0.0;
+      if (has_j && gl == 0 && t + 1 < D) di_next = __ldcg(B.dinit + (size_t)(t + 1) * N + j);
+      int ifine = 0;
+      bool amb = false;
+      long long bfine = 0;
+      if (has_j) {
+        // packed coarse matvec over i for slot t-1
+        int b1 = INT_MIN, b2 = INT_MIN;
+        const int* qrow = Qcp + j * Np;
+        const int* dv = dqcp + prv * Np;
+        for (int i4 = gl * 4; i4 < Np; i4 += 4 * G4) {
+          const int4 a = *reinterpret_cast<const int4*>(qrow + i4);
+          const int4 b = *reinterpret_cast<const int4*>(dv + i4);
+          packed_push(a.x + b.x, b1, b2);
+          packed_push(a.y + b.y, b1, b2);
+          packed_push(a.z + b.z, b1, b2);
+          packed_push(a.w + b.w, b1, b2);
+        }
 #pragma unroll
-      for (int o = HEAD_GROUP / 2; o > 0; o >>= 1) {
-        const long long ob1 = __shfl_xor_sync(gmask, tb.b1, o);
-        const long long ob2 = __shfl_xor_sync(gmask, tb.b2, o);
-        const int ox1 = __shfl_xor_sync(gmask, tb.x1, o);
-        tb.merge(ob1, ox1, ob2);
+        for (int o = G4 / 2; o > 0; o >>= 1) {
+          const int o1 = __shfl_xor_sync(gmask, b1, o);
+          const int o2 = __shfl_xor_sync(gmask, b2, o);
+          const int lo = min(b1, o1);
+          b1 = max(b1, o1);
+          b2 = max(max(b2, o2), lo);
+        }
+        ifine = 127 - (b1 & 127);
+        amb = ((b1 >> 7) - (b2 >> 7)) <= P.coarse_margin;
+        if (!amb) {
+          bfine = qtr[j * N + ifine] + dq[prv * N + ifine];
+        } else {
+          // fine int64 pass decides (and certifies with the fine margin)
+          Top2 tb;
+          tb.init();
+          for (int i = gl; i < N; i += G4) tb.push(qtr[j * N + i] + dq[prv * N + i], i);
+#pragma unroll
+          for (int o = G4 / 2; o > 0; o >>= 1) {
+            const long long ob1 = __shfl_xor_sync(gmask, tb.b1, o);
+            const long long ob2 = __shfl_xor_sync(gmask, tb.b2, o);
+            const int ox1 = __shfl_xor_sync(gmask, tb.x1, o);
+            tb.merge(ob1, ox1, ob2);
+          }
+          ifine = tb.x1;
+          bfine = tb.b1;
+          amb = (tb.b1 - tb.b2) <= m.margin;
+        }
+        if (gl == 0) {
+          ctil_h[hrow * N + j] = bfine - ptil[prv * N + j];
+          itil_h[hrow * N + j] = (unsigned short)(ifine | (amb ? 0x8000 : 0));
+        }
       }
-      if (t > D) {
-        // E_t[d] = E_{t-1}[d-1] + em_t, E_t[0] = 0 + em_t (src/hsmm.cu:298-310)
-        const double old = gl < L ? E_h[gl * N + j] : 0.0;
-        const double prev = __shfl_up_sync(gmask, old, 1, HEAD_GROUP);
-        if (gl < L) {
-          const double emt = m.em[(size_t)ot * N + j];
-          if (gl == 0) {
-            long long b = __double_as_longlong(emt);
-            E_h[j] = __longlong_as_double(b == (long long)0x8000000000000000ULL ? 0 : b);  // 0 + em_t
-          } else {
-            E_h[gl * N + j] = prev + emt;
+      cs_arrive();  // slot t-1 ready for the helpers
+      if (has_j) {
+        // the d = 0 candidate, exact (src/hsmm.cu:341-346 with E_t[0] = em_t)
+        ExactBest eb;
+        eb.init();
+        const double e0 = E[cur * L * N + j];
+        if (!amb) {
+          if (gl == 0)
+            eb.set((e0 + dstar_h[drow_prev * N + ifine]) + (m.trans[(size_t)j * N + ifine] + dur_h[j * L]), 0,
+                   ifine);
+        } else {
+          const double* row = dstar_h + drow_prev * N;
+          const double* trj = m.trans + (size_t)j * N;
+          for (int i = gl; i < N; i += G4) eb.offer((e0 + row[i]) + (trj[i] + dur_h[j * L]), 0, i);
+#pragma unroll
+          for (int o = G4 / 2; o > 0; o >>= 1) {
+            const long long ok = __shfl_xor_sync(gmask, eb.k, o);
+            const int od = __shfl_xor_sync(gmask, eb.d, o);
+            const int oi = __shfl_xor_sync(gmask, eb.i, o);
+            eb.offer_key(ok, od, oi);
           }
         }
-      } else if (gl == 0) {
-        // newest-first rebuild (src/hsmm.cu:311-322)
-        double gsum = m.em[(size_t)ot * N + j];
-        E_h[j] = gsum;
-        for (int d = 1; d < hl; ++d) {
-          gsum = gsum + m.em[(size_t)B.obs[t - d] * N + j];
-          E_h[d * N + j] = gsum;
-        }
-      }
-      unsigned long long* msg =
-          B.slot_msg + ((size_t)((unsigned)(t - 1) & (SLOT_RING - 1)) * N + j) * SLOT_WORDS;
-      const unsigned tag = (unsigned)t;  // slot t-1
-      const long long c = tb.b1 - ptil[j];
-      const bool amb = (tb.b1 - tb.b2) <= m.margin;
-      const unsigned short itv = (unsigned short)(tb.x1 | (amb ? 0x8000 : 0));
-      if (gl == 0) tagged64_store(msg, tag, (unsigned long long)c);
-      if (gl == 1)
-        tagged64_store(msg + 2, tag, (unsigned long long)__double_as_longlong(dstar_h[drow_prev * N + tb.x1]));
-      if (gl == 2) st_relaxed_u64(msg + 4, ((unsigned long long)tag << 32) | itv);
-      if (gl == 3) {
-        ctil_h[hrow * N + j] = c;
-        itil_h[hrow * N + j] = itv;
-      }
-      if (gl == 4) ptil[j] += m.qem[(size_t)ot * N + j];
-    }
-    if (tid < S) {
-      if (!msg_wait(B.part + ((size_t)((unsigned)t & (PART_RING - 1)) * S + tid) * 3, (unsigned)t, pm, B.abort_flag,
-                    P.timeout)) {
-        grid_fail(B, TV_ETIMEOUT_DEV, SITE_HEAD_PARTIAL);
-        s_fail = 1;
-      } else {
-        double v;
-        msg_unpack(pm, v, pd[tid], pi[tid]);
-        pk[tid] = order_key(v);
-      }
-    }
-    __syncthreads();
-    if (s_fail) return;
-
-    // Phase C: the head's candidates d < L, certified; merge; finalise.
-    if (has_j) {
-      Top2 tb;
-      tb.init();
-      if (gl < hl) tb.push(ctil_h[((hrow - gl) & (L - 1)) * N + j] + qd_h[j * L + gl], gl);
-#pragma unroll
-      for (int o = HEAD_GROUP / 2; o > 0; o >>= 1) {
-        const long long ob1 = __shfl_xor_sync(gmask, tb.b1, o);
-        const long long ob2 = __shfl_xor_sync(gmask, tb.b2, o);
-        const int ox1 = __shfl_xor_sync(gmask, tb.x1, o);
-        tb.merge(ob1, ox1, ob2);
-      }
-      const int d1 = tb.x1;
-      const unsigned short it = itil_h[((hrow - d1) & (L - 1)) * N + j];
-      const bool amb = (it & 0x8000) || ((tb.b1 - tb.b2) <= m.margin);
-      ExactBest eb;
-      eb.init();
-      if (!amb) {
         if (gl == 0) {
-          const int i1 = it & 0x7fff;
-          int dr = drow_prev - d1;
-          if (dr < 0) dr += L + 1;
-          eb.set((E_h[d1 * N + j] + dstar_h[dr * N + i1]) + (m.trans[(size_t)j * N + i1] + dur_h[j * L + d1]), d1,
-                 i1);
-        }
-      } else {
-        const long long thr = tb.b1 - m.margin;
-        if (gl < hl && ctil_h[((hrow - gl) & (L - 1)) * N + j] + qd_h[j * L + gl] >= thr) {
-          const int d = gl;
-          const double e = E_h[d * N + j];
-          const double du = dur_h[j * L + d];
-          int dr = drow_prev - d;
-          if (dr < 0) dr += L + 1;
-          const double* row = dstar_h + dr * N;
-          const double* trj = m.trans + (size_t)j * N;
-          for (int i = 0; i < N; ++i) eb.offer((e + row[i]) + (trj[i] + du), d, i);
-        }
-#pragma unroll
-        for (int o = HEAD_GROUP / 2; o > 0; o >>= 1) {
-          const long long ok = __shfl_xor_sync(gmask, eb.k, o);
-          const int od = __shfl_xor_sync(gmask, eb.d, o);
-          const int oi = __shfl_xor_sync(gmask, eb.i, o);
-          eb.offer_key(ok, od, oi);
+          eb.offer_key(prek[cur * N + j], pred[cur * N + j], prei[cur * N + j]);
+          double fin;
+          uint32_t wv;
+          // t < D: the induction result replaces the initialisation score only
+          // when strictly larger (src/hsmm.cu:353-358).
+          if (t >= D || eb.k > order_key(di_cur)) {
+            fin = eb.value();
+            wv = pack_psi(eb.d, eb.i);
+          } else {
+            fin = di_cur;
+            wv = pack_psi((int)t, 0);
+          }
+          dstar_h[drow * N + j] = fin;
+          const long long fq = quantize(fin, m.scale);
+          dq[cur * N + j] = fq;
+          dqcp[cur * Np + j] = coarse_of(fq - basebuf[cur], sh) * 128;
+          psirec[cur * N + j] = wv;
         }
       }
-      if (gl == 0) {
-        const int k0 = B.seg_first[j], k1 = k0 + B.seg_count[j];
-        for (int k = k0; k < k1; ++k)
-          if (pd[k] != EMPTY_D) eb.offer_key(pk[k], pd[k], pi[k]);
-        double fin;
-        uint32_t wv;
-        // t < D: the induction result replaces the initialisation score only
-        // when strictly larger (src/hsmm.cu:353-358).
-        if (t >= D || eb.k > order_key(di_cur)) {
-          fin = eb.value();
-          wv = pack_psi(eb.d, eb.i);
+      di_cur = di_next;
+    } else {
+      // ================= helper warps: prepare step t+1 =================
+      const long long t1 = t + 1;
+      const bool next = t1 < T;
+      const int nxt = cur ^ 1;  // (t+1) & 1
+      // worker partials of step t+1
+      if (next && hb < S) {
+        TaggedMsg pm;
+        msg_load(B.part + ((size_t)((unsigned)t1 & (PART_RING - 1)) * S + hb) * 3, pm);
+        if (!msg_wait(B.part + ((size_t)((unsigned)t1 & (PART_RING - 1)) * S + hb) * 3, (unsigned)t1, pm,
+                      B.abort_flag, P.timeout)) {
+          grid_fail(B, TV_ETIMEOUT_DEV, SITE_HEAD_PARTIAL);
+          s_fail = 1;
         } else {
-          fin = di_cur;
-          wv = pack_psi((int)t, 0);
+          double v;
+          msg_unpack(pm, v, pwd[hb], pwi[hb]);
+          pwk[hb] = order_key(v);
         }
-        dstar_h[drow * N + j] = fin;
-        tagged64_store(B.dstar + ((size_t)rdrow * N + j) * 2, (unsigned)(t + 1),
-                       (unsigned long long)__double_as_longlong(fin));
-        dq[j] = quantize(fin, m.scale);
-        B.psi[(size_t)t * N + j] = wv;
+      }
+      if (has_j) {
+        // window sums of step t+1
+        if (next) {
+          const int ot1 = B.obs[t1];
+          const double em1 = m.em[(size_t)ot1 * N + j];
+          if (t1 > D) {
+            // E_{t+1}[d] = E_t[d-1] + em_{t+1}, E_{t+1}[0] = 0 + em_{t+1} (src/hsmm.cu:298-310)
+            if (gl < L) {
+              if (gl == 0) {
+                const long long b = __double_as_longlong(em1);
+                E[nxt * L * N + j] = __longlong_as_double(b == (long long)0x8000000000000000ULL ? 0 : b);
+              } else {
+                E[(nxt * L + gl) * N + j] = E[(cur * L + gl - 1) * N + j] + em1;
+              }
+            }
+          } else if (gl == 0) {
+            // newest-first rebuild (src/hsmm.cu:311-322)
+            const int hl1 = (int)(t1 < L ? t1 : L);
+            double g = em1;
+            E[nxt * L * N + j] = g;
+            for (int d = 1; d < hl1; ++d) {
+              g = g + m.em[(size_t)B.obs[t1 - d] * N + j];
+              E[(nxt * L + d) * N + j] = g;
+            }
+          }
+        }
+        if (gl == 1) ptil[cur * N + j] = ptil[prv * N + j] + m.qem[(size_t)B.obs[t] * N + j];  // P(t)
+        // results of step t-1 to global memory
+        if (t >= 2) {
+          if (gl == 2) B.psi[(size_t)(t - 1) * N + j] = psirec[prv * N + j];
+          if (gl == 3)
+            tagged64_store(B.dstar + ((size_t)(rdrow == 0 ? P.Rd - 1 : rdrow - 1) * N + j) * 2, (unsigned)t,
+                           (unsigned long long)__double_as_longlong(dstar_h[drow_prev * N + j]));
+        }
+      }
+      // coarse base of step t+1: max_i delta[t-1] (the last helper warp)
+      if (hb >= GRID_THREADS - P.cs_threads - 32) {
+        const int l = hb - (GRID_THREADS - P.cs_threads - 32);
+        long long mx = LLONG_MIN;
+        for (int i = l; i < N; i += 32) mx = max(mx, dq[prv * N + i]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (l == 0) basebuf[nxt] = mx;
+      }
+      helper_wait_cs();  // the critical warps published slot t-1
+      if (has_j) {
+        // slot t-1 message for the workers
+        unsigned long long* msg =
+            B.slot_msg + ((size_t)((unsigned)(t - 1) & (SLOT_RING - 1)) * N + j) * SLOT_WORDS;
+        const unsigned tag = (unsigned)t;
+        const unsigned short itv = itil_h[hrow * N + j];
+        if (gl == 0) tagged64_store(msg, tag, (unsigned long long)ctil_h[hrow * N + j]);
+        if (gl == 1)
+          tagged64_store(msg + 2, tag,
+                         (unsigned long long)__double_as_longlong(dstar_h[drow_prev * N + (itv & 0x7fff)]));
+        if (gl == 2) st_relaxed_u64(msg + 4, ((unsigned long long)tag << 32) | itv);
+        if (next) {
+          // candidates d = 1..L-1 of step t+1 (slots t-d), certified, exact
+          const int tau1 = (int)(t1 < D ? t1 : D);
+          const int hl1 = tau1 < L ? tau1 : L;
+          Top2 tb;
+          tb.init();
+          const int dme = gl + 1;
+          if (dme < hl1) tb.push(ctil_h[((int)((t - dme) & (L - 1))) * N + j] + qd_h[j * L + dme], dme);
+#pragma unroll
+          for (int o = G4 / 2; o > 0; o >>= 1) {
+            const long long ob1 = __shfl_xor_sync(gmask, tb.b1, o);
+            const long long ob2 = __shfl_xor_sync(gmask, tb.b2, o);
+            const int ox1 = __shfl_xor_sync(gmask, tb.x1, o);
+            tb.merge(ob1, ox1, ob2);
+          }
+          ExactBest eb;
+          eb.init();
+          if (tb.x1 != IDX_NONE) {
+            const int d1 = tb.x1;
+            const unsigned short it = itil_h[((int)((t - d1) & (L - 1))) * N + j];
+            const bool amb = (it & 0x8000) || ((tb.b1 - tb.b2) <= m.margin);
+            if (!amb) {
+              if (gl == 0) {
+                const int i1 = it & 0x7fff;
+                int dr = drow_prev + 1 - d1;  // row of delta[t-d1]
+                if (dr < 0) dr += L + 1;
+                eb.set((E[(nxt * L + d1) * N + j] + dstar_h[dr * N + i1]) +
+                           (m.trans[(size_t)j * N + i1] + dur_h[j * L + d1]),
+                       d1, i1);
+              }
+            } else {
+              const long long thr = tb.b1 - m.margin;
+              if (dme < hl1 && ctil_h[((int)((t - dme) & (L - 1))) * N + j] + qd_h[j * L + dme] >= thr) {
+                const double e = E[(nxt * L + dme) * N + j];
+                const double du = dur_h[j * L + dme];
+                int dr = drow_prev + 1 - dme;
+                if (dr < 0) dr += L + 1;
+                const double* row = dstar_h + dr * N;
+                const double* trj = m.trans + (size_t)j * N;
+                for (int i = 0; i < N; ++i) eb.offer((e + row[i]) + (trj[i] + du), dme, i);
+              }
+#pragma unroll
+              for (int o = G4 / 2; o > 0; o >>= 1) {
+                const long long ok = __shfl_xor_sync(gmask, eb.k, o);
+                const int od = __shfl_xor_sync(gmask, eb.d, o);
+                const int oi = __shfl_xor_sync(gmask, eb.i, o);
+                eb.offer_key(ok, od, oi);
+              }
+            }
+          }
+          if (gl == 0) {
+            const int k0 = B.seg_first[j], k1 = k0 + B.seg_count[j];
+            for (int k = k0; k < k1; ++k)
+              if (pwd[k] != EMPTY_D) eb.offer_key(pwk[k], pwd[k], pwi[k]);
+            prek[nxt * N + j] = eb.k;
+            pred[nxt * N + j] = eb.d;
+            prei[nxt * N + j] = eb.i;
+          }
+        }
       }
     }
-    di_cur = di_next;
-    pm = pm_next;
-    hrow = (hrow + 1) & (L - 1);
     drow_prev = drow;
     rdrow = rdrow + 1 == P.Rd ? 0 : rdrow + 1;
     __syncthreads();
+    if (s_fail) return;
   }
 
   // Tail at t = T-1 (src/hsmm.cu:101-137).
@@ -618,34 +807,36 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
     const int tau = (int)(t < D ? t : D);
     const int hl = tau < L ? tau : L;
     if (tid < S) {
+      TaggedMsg pm;
+      msg_load(B.part + ((size_t)((unsigned)T & (PART_RING - 1)) * S + tid) * 3, pm);
       if (!msg_wait(B.part + ((size_t)((unsigned)T & (PART_RING - 1)) * S + tid) * 3, (unsigned)T, pm, B.abort_flag,
                     P.timeout)) {
         grid_fail(B, TV_ETIMEOUT_DEV, SITE_HEAD_TAIL);
         s_fail = 1;
       } else {
         double v;
-        msg_unpack(pm, v, pd[tid], pi[tid]);
-        pk[tid] = order_key(v);
+        msg_unpack(pm, v, pwd[tid], pwi[tid]);
+        pwk[tid] = order_key(v);
       }
     }
     __syncthreads();
     if (s_fail) return;
-    if (has_j) {
+    if (is_cs && has_j) {
       ExactBest eb;
       eb.init();
-      if (gl < hl) {
-        const int d = gl;
-        const double e = E_h[d * N + j] + m.survT[(size_t)j * D + d];
+      const int ec = (int)(t & 1);
+      for (int d = gl; d < hl; d += G4) {
+        const double e = E[(ec * L + d) * N + j] + m.survT[(size_t)j * D + d];
         // after the loop drow_prev is the row of delta[T-1]; the tail reads
         // delta[t-1-d] = delta[T-2-d]
         int dr = drow_prev - 1 - d;
-        if (dr < 0) dr += L + 1;
+        while (dr < 0) dr += L + 1;
         const double* row = dstar_h + dr * N;
         const double* trj = m.trans + (size_t)j * N;
         for (int i = 0; i < N; ++i) eb.offer((e + row[i]) + trj[i], d, i);
       }
 #pragma unroll
-      for (int o = HEAD_GROUP / 2; o > 0; o >>= 1) {
+      for (int o = G4 / 2; o > 0; o >>= 1) {
         const long long ok = __shfl_xor_sync(gmask, eb.k, o);
         const int od = __shfl_xor_sync(gmask, eb.d, o);
         const int oi = __shfl_xor_sync(gmask, eb.i, o);
@@ -654,7 +845,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
       if (gl == 0) {
         const int k0 = B.seg_first[j], k1 = k0 + B.seg_count[j];
         for (int k = k0; k < k1; ++k)
-          if (pd[k] != EMPTY_D) eb.offer_key(pk[k], pd[k], pi[k]);
+          if (pwd[k] != EMPTY_D) eb.offer_key(pwk[k], pwd[k], pwi[k]);
         if (eb.d == IDX_NONE) { eb.d = 0; eb.i = 0; }
         tail[j] = eb.value();
         B.psi[(size_t)t * N + j] = pack_psi(eb.d, eb.i);

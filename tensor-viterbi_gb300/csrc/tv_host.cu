@@ -342,19 +342,30 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, tv::GridParams& P, std::vec
   P.w_red = o;  o = tv::tv_align(o + (unsigned long long)std::max(max_seg * (tv::WORKER_THREADS / 32) * sizeof(tv::Top2), 32 * sizeof(tv::ExactBest)));
   P.w_bytes = o;
   o = 0;
-  P.h_qtr = o;   o = tv::tv_align(o + (unsigned long long)N * N * 8);
-  P.h_ctil = o;  o = tv::tv_align(o + (unsigned long long)L * N * 8);
-  P.h_itil = o;  o = tv::tv_align(o + (unsigned long long)L * N * 2);
-  P.h_dstar = o; o = tv::tv_align(o + (unsigned long long)(L + 1) * N * 8);
-  P.h_E = o;     o = tv::tv_align(o + (unsigned long long)L * N * 8);
-  P.h_qd = o;    o = tv::tv_align(o + (unsigned long long)N * L * 8);
-  P.h_dur = o;   o = tv::tv_align(o + (unsigned long long)N * L * 8);
-  P.h_dq = o;    o = tv::tv_align(o + (unsigned long long)N * 8);
-  P.h_ptil = o;  o = tv::tv_align(o + (unsigned long long)N * 8);
-  P.h_pv = o;    o = tv::tv_align(o + (unsigned long long)S * 8);  // order keys
-  P.h_pd = o;    o = tv::tv_align(o + (unsigned long long)S * 4);
-  P.h_pi = o;    o = tv::tv_align(o + (unsigned long long)S * 4);
-  P.h_tail = o;  o = tv::tv_align(o + (unsigned long long)N * 8);
+  const int Np = (N + 15) / 16 * 16;
+  P.Np = Np;
+  P.cs_threads = (tv::HEAD_GROUP * N + 31) / 32 * 32;
+  if (tv::GRID_THREADS - P.cs_threads < tv::HEAD_GROUP * N || tv::GRID_THREADS - P.cs_threads < 32) return false;
+  P.h_qcp = o;    o = tv::tv_align(o + (unsigned long long)N * Np * 4);
+  P.h_qtr = o;    o = tv::tv_align(o + (unsigned long long)N * N * 8);
+  P.h_dqcp = o;   o = tv::tv_align(o + (unsigned long long)2 * Np * 4);
+  P.h_dq = o;     o = tv::tv_align(o + (unsigned long long)2 * N * 8);
+  P.h_ptil = o;   o = tv::tv_align(o + (unsigned long long)2 * N * 8);
+  P.h_base = o;   o = tv::tv_align(o + 16);
+  P.h_dstar = o;  o = tv::tv_align(o + (unsigned long long)(L + 1) * N * 8);
+  P.h_ctil = o;   o = tv::tv_align(o + (unsigned long long)L * N * 8);
+  P.h_itil = o;   o = tv::tv_align(o + (unsigned long long)L * N * 2);
+  P.h_E = o;      o = tv::tv_align(o + (unsigned long long)2 * L * N * 8);
+  P.h_qd = o;     o = tv::tv_align(o + (unsigned long long)N * L * 8);
+  P.h_dur = o;    o = tv::tv_align(o + (unsigned long long)N * L * 8);
+  P.h_prek = o;   o = tv::tv_align(o + (unsigned long long)2 * N * 8);
+  P.h_pred = o;   o = tv::tv_align(o + (unsigned long long)2 * N * 4);
+  P.h_prei = o;   o = tv::tv_align(o + (unsigned long long)2 * N * 4);
+  P.h_pwk = o;    o = tv::tv_align(o + (unsigned long long)S * 8);
+  P.h_pwd = o;    o = tv::tv_align(o + (unsigned long long)S * 4);
+  P.h_pwi = o;    o = tv::tv_align(o + (unsigned long long)S * 4);
+  P.h_psirec = o; o = tv::tv_align(o + (unsigned long long)2 * N * 4);
+  P.h_tail = o;   o = tv::tv_align(o + (unsigned long long)N * 8);
   P.h_bytes = o;
   P.timeout = 1LL << 31;  // SM clock cycles, about a second: no legitimate wait comes close
   return std::max(P.w_bytes, P.h_bytes) + 256 <= (unsigned long long)smem_optin;
@@ -364,6 +375,7 @@ int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_
                 cudaStream_t st, const tv::GridParams& P) {
   const int N = m->N, D = m->D;
   const Quant Q = choose_quant(m, T);
+  if (Q.f < tv::COARSE_F) return fail(TV_ETOOBIG, "sequence too long for the grid kernel's fixed-point range");
   int rc;
   if ((rc = prepare_quant(m, Q, st)) != TV_OK) return rc;
   if ((rc = m->psi.ensure((size_t)T * N)) != TV_OK) return rc;
@@ -409,6 +421,16 @@ int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_
   B.status = gstatus;
   B.site = m->gflags.p + 0;
   tv::GridParams Pc = P;
+  // Packed coarse matvec: coarse unit 2^-COARSE_F.  Each coarse score is off
+  // by < 2 units (two floors) from the fine one, which is within q + 3uS of
+  // the exact value; a coarse runner-up gap above the margin certifies the
+  // argmax over i.
+  Pc.coarse_shift = Q.f - tv::COARSE_F;
+  {
+    const double u = std::ldexp(1.0, -53), q = std::ldexp(1.0, -Q.f), qc = std::ldexp(1.0, -tv::COARSE_F);
+    const double S_ = (double)T * (m->emax + m->tmax + m->dmax) + m->smax + (double)m->D * m->emax + m->tmax + m->dmax;
+    Pc.coarse_margin = 4 + (int)std::ceil(2.0 * (q + 3.0 * u * S_) / qc) + 2;
+  }
   void* args[] = {&mv, &Pc, &B};
   const size_t dyn = std::max(P.w_bytes, P.h_bytes);
   TV_CUDA(cudaFuncSetAttribute(tv::grid_decode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
