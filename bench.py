@@ -325,8 +325,11 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="single_N75_D5000_T1e6")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--T", type=int, default=0, help="override the sequence length (profiling runs)")
     args = ap.parse_args()
-    w = WORKLOADS[args.workload]
+    w = dict(WORKLOADS[args.workload])
+    if args.T:
+        w["T"] = args.T
     if args.impl == "reference":
         return run_reference(args, w, args.workload)
     return run_ours(args, w, args.workload)

@@ -685,12 +685,12 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
           const double em1 = m.em[(size_t)ot1 * N + j];
           if (t1 > D) {
             // E_{t+1}[d] = E_t[d-1] + em_{t+1}, E_{t+1}[0] = 0 + em_{t+1} (src/hsmm.cu:298-310)
-            if (gl < L) {
-              if (gl == 0) {
+            for (int d = gl; d < L; d += G4) {
+              if (d == 0) {
                 const long long b = __double_as_longlong(em1);
                 E[nxt * L * N + j] = __longlong_as_double(b == (long long)0x8000000000000000ULL ? 0 : b);
               } else {
-                E[(nxt * L + gl) * N + j] = E[(cur * L + gl - 1) * N + j] + em1;
+                E[(nxt * L + d) * N + j] = E[(cur * L + d - 1) * N + j] + em1;
               }
             }
           } else if (gl == 0) {
@@ -740,8 +740,8 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
           const int hl1 = tau1 < L ? tau1 : L;
           Top2 tb;
           tb.init();
-          const int dme = gl + 1;
-          if (dme < hl1) tb.push(ctil_h[((int)((t - dme) & (L - 1))) * N + j] + qd_h[j * L + dme], dme);
+          for (int dme = gl + 1; dme < hl1; dme += G4)
+            tb.push(ctil_h[((int)((t - dme) & (L - 1))) * N + j] + qd_h[j * L + dme], dme);
 #pragma unroll
           for (int o = G4 / 2; o > 0; o >>= 1) {
             const long long ob1 = __shfl_xor_sync(gmask, tb.b1, o);
@@ -766,7 +766,8 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
               }
             } else {
               const long long thr = tb.b1 - m.margin;
-              if (dme < hl1 && ctil_h[((int)((t - dme) & (L - 1))) * N + j] + qd_h[j * L + dme] >= thr) {
+              for (int dme = gl + 1; dme < hl1; dme += G4) {
+                if (ctil_h[((int)((t - dme) & (L - 1))) * N + j] + qd_h[j * L + dme] < thr) continue;
                 const double e = E[(nxt * L + dme) * N + j];
                 const double du = dur_h[j * L + dme];
                 int dr = drow_prev + 1 - dme;
