@@ -47,6 +47,7 @@ struct BatchView {
   uint32_t* psi;          // concatenated (T_k, N) back-pointer words
   int* status;            // (n_seq)
   int* next;              // work-queue counter, zero at launch
+  const int* order;       // queue order (longest first), or null for 0..n_seq-1
   int n_seq;
 };
 
@@ -60,7 +61,7 @@ struct CtaLayout {
 __host__ __device__ inline unsigned long long tv_align(unsigned long long x) { return (x + 15ull) & ~15ull; }
 
 __host__ inline CtaLayout make_cta_layout(int N, int D) {
-  CtaLayout L;
+  CtaLayout L{};
   unsigned long long o = 0;
   const unsigned long long nd = (unsigned long long)N * D;
   L.o_qd = o;    o = tv_align(o + nd * 8);
@@ -131,7 +132,10 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
 
   for (;;) {
     __syncthreads();
-    if (threadIdx.x == 0) s_seq = atomicAdd(b.next, 1);
+    if (threadIdx.x == 0) {
+      const int k = atomicAdd(b.next, 1);
+      s_seq = k < b.n_seq ? (b.order ? b.order[k] : k) : b.n_seq;
+    }
     __syncthreads();
     const int seq = s_seq;
     if (seq >= b.n_seq) break;

@@ -111,6 +111,7 @@ struct tv_model_s {
   DevBuf<int> status;
   DevBuf<int> counter;
   DevBuf<int64_t> off;
+  DevBuf<int> order;
   DevBuf<unsigned char> scratch;
   DevBuf<int32_t> obs_tmp, path_tmp;
   DevBuf<double> ll_tmp;
@@ -188,7 +189,7 @@ int prepare_quant(tv_model_s* m, const Quant& Q, cudaStream_t st) {
 }
 
 tv::ModelView view(const tv_model_s* m, const Quant& Q) {
-  tv::ModelView v;
+  tv::ModelView v{};
   v.N = m->N; v.O = m->O; v.D = m->D;
   v.em = m->em.p; v.trans = m->trans.p; v.start = m->start.p;
   v.durT = m->durT.p; v.survT = m->survT.p;
@@ -230,6 +231,19 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
   if ((rc = m->off.ensure((size_t)n_seq + 1)) != TV_OK) return rc;
   TV_CUDA(cudaMemcpyAsync(m->off.p, off_host, sizeof(int64_t) * (n_seq + 1), cudaMemcpyHostToDevice, st));
   TV_CUDA(cudaMemsetAsync(m->counter.p, 0, sizeof(int), st));
+  // Longest sequences first: the persistent CTAs then finish close together.
+  const int* order_dev = nullptr;
+  if (n_seq > 1) {
+    std::vector<int> ord((size_t)n_seq);
+    for (int k = 0; k < n_seq; ++k) ord[k] = k;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+      return off_host[a + 1] - off_host[a] > off_host[b + 1] - off_host[b];
+    });
+    if ((rc = m->order.ensure((size_t)n_seq)) != TV_OK) return rc;
+    // pageable source: the copy is staged before the call returns
+    TV_CUDA(cudaMemcpyAsync(m->order.p, ord.data(), sizeof(int) * n_seq, cudaMemcpyHostToDevice, st));
+    order_dev = m->order.p;
+  }
 
   tv::CtaLayout L = tv::make_cta_layout(N, D);
   int dev = 0;
@@ -254,7 +268,7 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
     if ((rc = m->scratch.ensure((size_t)grid * L.bytes)) != TV_OK) return rc;
     scratch = m->scratch.p;
   }
-  tv::BatchView bv;
+  tv::BatchView bv{};
   bv.obs = obs_dev;
   bv.off = m->off.p;
   bv.path = path_dev;
@@ -262,6 +276,7 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
   bv.psi = m->psi.p;
   bv.status = m->status.p;
   bv.next = m->counter.p;
+  bv.order = order_dev;
   bv.n_seq = n_seq;
   mark_start(m, st);
   kern<<<grid, kThreads, dyn, st>>>(view(m, Q), bv, L, scratch);
@@ -402,7 +417,7 @@ int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_
     m->last_launches += 1;
   }
   TV_CUDA(cudaGetLastError());
-  tv::GridBufs B;
+  tv::GridBufs B{};
   B.obs = obs_dev;
   B.T = T;
   B.psi = m->psi.p;
@@ -631,7 +646,7 @@ int tv_model_destroy(tv_model m) {
   if (!m) return TV_OK;
   m->em.release(); m->trans.release(); m->start.release(); m->durT.release(); m->survT.release();
   m->qem.release(); m->qtr.release(); m->qdurT.release();
-  m->psi.release(); m->status.release(); m->counter.release(); m->off.release(); m->scratch.release();
+  m->psi.release(); m->status.release(); m->counter.release(); m->off.release(); m->order.release(); m->scratch.release();
   m->msgs.release(); m->dinit.release(); m->ck.release(); m->wrange.release();
   m->seg_first.release(); m->seg_count.release(); m->seg_base.release(); m->gflags.release();
   if (m->ev0) cudaEventDestroy(m->ev0);
@@ -803,7 +818,7 @@ int tv_decode_device_static(tv_model m, const int32_t* obs_dev, int64_t T, int32
   v.qem = qem;
   v.qtr = qtr;
   v.qdurT = qd;
-  tv::BatchView bv;
+  tv::BatchView bv{};
   bv.obs = obs_dev;
   bv.off = off;
   bv.path = path_dev;
@@ -811,6 +826,7 @@ int tv_decode_device_static(tv_model m, const int32_t* obs_dev, int64_t T, int32
   bv.psi = psi;
   bv.status = status;
   bv.next = counter;
+  bv.order = nullptr;
   bv.n_seq = 1;
   tv::cta_decode_kernel<kThreads><<<1, kThreads, L.bytes, st>>>(v, bv, L, nullptr);
   if (status_dev) static_status_kernel<<<1, 1, 0, st>>>(status, status_dev);

@@ -193,17 +193,53 @@ def batch_lengths(n_seq: int = 4096, lo: float = 1e3, hi: float = 1e5, seed: int
     return np.exp(rng.uniform(math.log(lo), math.log(hi), size=n_seq)).astype(np.int64)
 
 
+def sample_states_batch(rng: np.random.Generator, lm: LinearModel, lengths) -> list:
+    """Hidden state paths for many sequences at once: every iteration draws the
+    next segment (duration, then successor state) of all unfinished sequences
+    together.  Same model family as sample_states."""
+    N, D = lm.P.shape
+    lengths = np.asarray(lengths, dtype=np.int64)
+    K = lengths.size
+    cdfP = np.cumsum(lm.P, axis=1)
+    cdfP /= cdfP[:, -1:]
+    cdfA = np.cumsum(lm.A, axis=1)
+    cdfA /= cdfA[:, -1:]
+    cdfpi = np.cumsum(lm.pi)
+    cdfpi /= cdfpi[-1]
+    state = np.minimum(np.searchsorted(cdfpi, rng.random(K), side="right"), N - 1)
+    pos = np.zeros(K, dtype=np.int64)
+    seg_starts = [[] for _ in range(K)]
+    seg_states = [[] for _ in range(K)]
+    active = np.arange(K)
+    while active.size:
+        st = state[active]
+        u = rng.random(active.size)
+        dur = np.minimum((u[:, None] >= cdfP[st]).sum(axis=1), D - 1) + 1
+        for k, a in enumerate(active):
+            seg_starts[a].append(pos[a])
+            seg_states[a].append(st[k])
+        pos[active] += dur
+        u = rng.random(active.size)
+        state[active] = np.minimum((u[:, None] >= cdfA[st]).sum(axis=1), N - 1)
+        active = active[pos[active] < lengths[active]]
+    out = []
+    for a in range(K):
+        starts = np.asarray(seg_starts[a] + [lengths[a]], dtype=np.int64)
+        reps = np.minimum(np.diff(starts), lengths[a] - starts[:-1])
+        out.append(np.repeat(np.asarray(seg_states[a], dtype=np.int32), np.maximum(reps, 0))[: lengths[a]])
+    return out
+
+
 def batch_problem(n_seq: int = 4096, N: int = 10, D: int = 250, M: int = 16, lo: float = 1e3, hi: float = 1e5,
                   seed: int = 2):
-    """One shared model, n_seq sequences with log-uniform lengths, each
-    sampled with its own seed.  Returns (Problem with an empty obs, [obs])."""
+    """One shared model, n_seq sequences with log-uniform lengths.  Returns
+    (Problem with an empty obs, [obs])."""
     rng = np.random.default_rng(seed)
     lm = random_model(rng, N, D, M, 5.0, 50.0)
     lengths = batch_lengths(n_seq, lo, hi, seed)
-    seqs = []
-    for k, T in enumerate(lengths):
-        r = np.random.default_rng([seed, k])
-        st = sample_states(r, lm, int(T))
-        seqs.append(sample_discrete_obs(r, lm.B, st))
+    states = sample_states_batch(rng, lm, lengths)
+    flat = np.concatenate(states)
+    obs_flat = sample_discrete_obs(rng, lm.B, flat)
+    seqs = np.split(obs_flat, np.cumsum(lengths)[:-1])
     prob = to_problem(lm, np.zeros(0, dtype=np.int32), meta=dict(N=N, D=D, M=M, n_seq=n_seq, seed=seed))
-    return prob, seqs
+    return prob, [np.ascontiguousarray(s) for s in seqs]
