@@ -105,4 +105,27 @@ __device__ __forceinline__ long long quantize(double x, double scale) {
   return __double2ll_rn(x * scale);
 }
 
+// round-half-even(x * 2^f) from the bits of x, on the integer pipes; equal to
+// quantize(x, 2^f) for every finite x whose scaled value fits in int64.
+__device__ __forceinline__ long long fixed_from_double(double x, int f) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((bits >> 52) & 0x7ff);
+  if (e == 0) return 0;  // zero or subnormal: |x * 2^f| < 1/2
+  const long long M = (long long)((bits & 0xfffffffffffffull) | (1ull << 52));
+  const int sh = e - 1075 + f;
+  long long q;
+  if (sh >= 0) {
+    q = M << sh;
+  } else if (sh < -54) {
+    q = 0;
+  } else {
+    const int r = -sh;
+    q = M >> r;
+    const long long rem = M & ((1LL << r) - 1);
+    const long long half = 1LL << (r - 1);
+    q += (rem > half || (rem == half && (q & 1))) ? 1 : 0;
+  }
+  return (bits >> 63) ? -q : q;
+}
+
 }  // namespace tv

@@ -39,9 +39,9 @@
 
 namespace tv {
 
-constexpr int GRID_THREADS = 1024;   // the head uses all of them
+constexpr int GRID_THREADS = 768;    // largest block: the head's roles for N <= 128
 constexpr int WORKER_THREADS = 256;  // a worker CTA keeps 8 warps; the rest exit at once
-constexpr int GRID_L = 4;            // head candidates d < L (a power of two)
+constexpr int GRID_L = 8;            // head candidates d < L (a power of two)
 constexpr int CK_STRIDE = 32;      // checkpoint stride of the early window sums
 constexpr int PART_RING = 32;      // steps of worker partials in flight
 constexpr int SLOT_RING = 64;      // slot messages kept
@@ -57,10 +57,16 @@ struct GridParams {
   int G, L, S, Rd, M;
   long long chunk;  // largest worker range, in cells
   int max_seg;
-  unsigned long long w_qd, w_dur, w_tr, w_ctil, w_dsel, w_acc0, w_acc1, w_itil, w_red, w_bytes;
+  unsigned long long w_qd, w_dur, w_tr, w_ctil, w_dsel, w_acc0, w_acc1, w_itil, w_red, w_emw, w_bytes;
   // head shared-memory offsets
-  unsigned long long h_qcp, h_qtr, h_dqcp, h_dq, h_ptil, h_base, h_dstar, h_ctil, h_itil, h_E, h_qd, h_dur, h_prek,
-      h_pred, h_prei, h_pwk, h_pwd, h_pwi, h_psirec, h_tail, h_bytes;
+  unsigned long long h_qcp, h_qtr, h_trh, h_dqcp, h_dq, h_ptil, h_base, h_dstar, h_ctil, h_itil, h_hwr, h_qd, h_dur,
+      h_prek, h_pred, h_prei, h_prew, h_preq, h_pwq, h_pwk, h_pwd, h_pwi, h_psirec, h_tail, h_bytes;
+  int trans_smem;     // the exact transition matrix is kept in the head's shared memory
+  int cs_dense;       // critical threads of the dense (one lane per state) phase: N rounded up to 32
+  int st_threads;     // state helper threads: N rounded up to 32
+  int in_threads;     // intake threads: S rounded up to 32
+  int block;          // threads per CTA: the head's roles (at least WORKER_THREADS)
+  int qf;             // fraction bits of the fixed-point scores
   int Np;             // N rounded up to 16 (packed coarse matvec rows)
   int cs_threads;     // critical-section threads (4 lanes per state, whole warps)
   int coarse_shift;   // fine-to-coarse right shift (f - COARSE_F)
@@ -79,6 +85,7 @@ struct GridBufs {
   unsigned long long* dstar;    // [Rd][N][2] tagged exact delta ring
   const double* dinit;          // [D][N] initialisation scores
   const double* ck;             // [D][M][N] checkpoints of the early window sums
+  const double* hwin;           // [T][L][N] window sums E_t[d], d < L
   const long long* wrange;      // [G-1][2] worker cell ranges
   const int* seg_first;         // [N]
   const int* seg_count;         // [N]
@@ -96,6 +103,47 @@ __device__ __forceinline__ double early_window(const ModelView& m, const double*
   double g = ck[((size_t)(t - 1) * M + q) * m.N + j];
   for (int k = q * CK_STRIDE + 1; k <= d; ++k) g = g + m.em[(size_t)obs[t - k] * m.N + j];
   return g;
+}
+
+// Window sum E_t[d] (d < min(t, D)) as the reference holds it at step t, from
+// an accessor em(s) of the emission values: newest-first while t <= D
+// (src/hsmm.cu:311-322); after that the rolling fold E_t[d] = E_{t-1}[d-1] +
+// em_t (src/hsmm.cu:298-310) unrolled back to where it began: 0 + em_{t-d}
+// then oldest-first, or, when it reaches back to step D, the newest-first sum
+// of step D then oldest-first.
+template <class F>
+__device__ __forceinline__ double window_sum(F em, int D, long long t, int d) {
+  double g;
+  if (t <= D) {
+    g = em(t);
+    for (int k = 1; k <= d; ++k) g = g + em(t - k);
+    return g;
+  }
+  long long s0 = t - d;
+  if (s0 > D) {
+    g = 0.0 + em(s0);
+  } else {
+    const int dd = d - (int)(t - D);
+    g = em(D);
+    for (int k = 1; k <= dd; ++k) g = g + em(D - k);
+    s0 = D;
+  }
+  for (long long s = s0 + 1; s <= t; ++s) g = g + em(s);
+  return g;
+}
+
+// The head's window sums E_t[d] for d < L at every step, [T][L][N] (zero where
+// d >= min(t, D)): read a few steps ahead by the head instead of folded on
+// its critical path.
+__global__ void grid_prep_hwin(ModelView m, const int32_t* obs, long long T, double* hwin, const int* abort_flag) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= T * m.N || *abort_flag) return;
+  const long long t = idx / m.N;
+  const int j = (int)(idx % m.N);
+  const int tau = (int)(t < m.D ? t : m.D);
+  auto em = [&](long long s) { return m.em[(size_t)obs[s] * m.N + j]; };
+  double* out = hwin + (size_t)t * GRID_L * m.N + j;
+  for (int d = 0; d < GRID_L; ++d) out[(size_t)d * m.N] = d < tau ? window_sum(em, m.D, t, d) : 0.0;
 }
 
 // Observations may come straight from device memory: a value outside [0, O)
@@ -157,8 +205,11 @@ __device__ __forceinline__ bool load_dstar(const GridBufs& B, const GridParams& 
 }
 
 // Named barrier of the worker threads only (the rest of the CTA has exited).
+// The non-aligned barrier counts threads, so lanes of a warp may arrive apart
+// (after a lane-0 wait, say); the aligned bar.sync would need the warp
+// converged, which the compiler does not ensure before inline assembly.
 __device__ __forceinline__ void worker_sync() {
-  asm volatile("bar.sync 1, %0;" ::"r"(WORKER_THREADS) : "memory");
+  asm volatile("barrier.sync 1, %0;" ::"r"(WORKER_THREADS) : "memory");
 }
 
 // Block-wide reduction of an ExactBest over the worker threads; every worker
@@ -181,7 +232,7 @@ __device__ __forceinline__ void send_partial(const GridBufs& B, const GridParams
   TaggedMsg msg;
   const bool empty = eb.d == IDX_NONE;
   msg_pack(msg, tag, eb.value(), empty ? EMPTY_D : eb.d, empty ? 0 : eb.i);
-  msg_store(B.part + ((size_t)ring * P.S + seg) * 3, msg);
+  msg_store(B.part + ((size_t)ring * P.S + seg) * MSG_WORDS, msg);
 }
 
 // ---------------------------------------------------------------------------
@@ -210,6 +261,7 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
   unsigned short* itil = (unsigned short*)(sm + P.w_itil);
   Top2* red = (Top2*)(sm + P.w_red);                  // [nseg][NW]
   ExactBest* ered = (ExactBest*)(sm + P.w_red);
+  double* emw = (double*)(sm + P.w_emw);              // [2][max_seg] emission of the fold's step
   __shared__ int s_bad;
 
   for (long long k = tid; k < (long long)nseg * D; k += WORKER_THREADS) {
@@ -225,23 +277,52 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
     re = (s == nseg - 1) ? (int)(c_hi - (long long)jb * D) : D;
   };
 
+  // Emission values of the fold's step, loaded ahead: emw holds step t+1
+  // while step t runs; thread s (< nseg) keeps step t+2's value and step
+  // t+3's observation in registers.
+  double em_pf = 0.0;
+  int ob_pf = 0;
+  if (tid < nseg) {
+    const int j = ja + tid;
+    if (2 < T) emw[tid] = m.em[(size_t)B.obs[2] * N + j];
+    if (3 < T) em_pf = m.em[(size_t)B.obs[3] * N + j];
+    if (4 < T) ob_pf = B.obs[4];
+  }
+  worker_sync();
+
   int r0 = 0;  // (t-1) % D
   for (long long t = 1; t < T; ++t) {
     const int tau = (int)(t < D ? t : D);
     const unsigned prow = (unsigned)t & (PART_RING - 1);
+    const long long t1 = t + 1;
+    int r0n = r0 + 1;  // t % D: the slot that enters at step t+1 (d = 0 then)
+    if (r0n == D) r0n = 0;
+    if (tid < nseg) {
+      if (t + 2 < T) emw[(int)((t + 2) & 1) * P.max_seg + tid] = em_pf;
+      if (t + 3 < T) em_pf = m.em[(size_t)ob_pf * N + ja + tid];
+      if (t + 4 < T) ob_pf = B.obs[t + 4];
+    }
 
-    // Phase 1: fixed-point scan over d in [L, tau).
+    // Phase 1: fixed-point scan over d in [L, tau), fused with the exact
+    // window folds of step t+1 into the other buffer (src/hsmm.cu:298-310):
+    // E_{t+1}[d] = E_t[d-1] + em_{t+1}, E_{t+1}[0] = 0 + em_{t+1}.  The FP64
+    // adds overlap the integer scan.
+    const bool fold = (t1 < T) && (t1 > D + 1);
     for (int s = 0; s < nseg; ++s) {
       int rb, re;
       seg_of(s, rb, re);
       const long long* ct = ctil + s * D - off0;
       const long long* q = qd + s * D;
+      const double* ac = acc_cur + s * D - off0;
+      double* an = acc_nxt + s * D - off0;
+      const double em1 = fold ? emw[(int)(t1 & 1) * P.max_seg + s] : 0.0;
       Top2 tb;
       tb.init();
       for (int r = rb + tid; r < re; r += WORKER_THREADS) {
         int d = r0 - r;
         if (d < 0) d += D;
         if (d >= L && d < tau) tb.push(ct[r] + q[d], d);
+        if (fold) an[r] = ((r == r0n) ? 0.0 : ac[r]) + em1;
       }
       tb.warp_reduce();
       if (lane == 0) red[s * NW + warp] = tb;
@@ -342,39 +423,28 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
         }
       }
     }
-    // Phase 2c: exact window folds of step t+1 into the other buffer,
-    // E_{t+1}[d] = E_t[d-1] + em_{t+1}, E_{t+1}[0] = 0 + em_{t+1}
-    // (src/hsmm.cu:298-310); at t+1 = D+1 seeded from the reference's
-    // newest-first sums of step D.
-    int r0n = r0 + 1;
-    if (r0n == D) r0n = 0;
-    const long long t1 = t + 1;
-    const bool fold = (t1 < T) && (t1 > D);
-    if (fold) {
+    // Phase 2c: at t+1 = D+1 the first fold starts from the reference's
+    // newest-first sums of step D: E_{D+1}[d] = E_D[d-1] + em_{D+1}.
+    const bool seed = (t1 < T) && (t1 == D + 1);
+    if (seed) {
       const int ot1 = B.obs[t1];
       for (int s = 0; s < nseg; ++s) {
         int rb, re;
         seg_of(s, rb, re);
         const int j = ja + s;
         const double em1 = m.em[(size_t)ot1 * N + j];
-        const double* ac = acc_cur + s * D - off0;
         double* an = acc_nxt + s * D - off0;
-        if (t1 == D + 1) {
-          for (int r = rb + tid; r < re; r += WORKER_THREADS) {
-            int d = r0n - r;
-            if (d < 0) d += D;
-            const double base = (d == 0) ? 0.0 : early_window(m, B.ck, P.M, B.obs, D, d - 1, j);
-            an[r] = base + em1;
-          }
-        } else {
-          for (int r = rb + tid; r < re; r += WORKER_THREADS)
-            an[r] = ((r == r0n) ? 0.0 : ac[r]) + em1;
+        for (int r = rb + tid; r < re; r += WORKER_THREADS) {
+          int d = r0n - r;
+          if (d < 0) d += D;
+          const double base = (d == 0) ? 0.0 : early_window(m, B.ck, P.M, B.obs, D, d - 1, j);
+          an[r] = base + em1;
         }
       }
     }
     worker_sync();
     if (s_bad) return;
-    if (fold) {
+    if (fold || seed) {
       double* x = acc_cur;
       acc_cur = acc_nxt;
       acc_nxt = x;
@@ -422,26 +492,51 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
 // ---------------------------------------------------------------------------
 // Head CTA
 //
-// The serial critical path of a step is: the scores delta[t-1] are final ->
-// B[t-1][j] = max_i(trans[j][i] + delta[t-1][i]) for every j -> the d = 0
-// candidate -> merge with everything else -> delta[t].  Only that chain runs
-// in the critical warps (4 lanes per state, the first cs_threads threads):
-//   * the matvec in packed int32: coarse score << 7 | (127 - i), so one
-//     integer max yields the value and the lowest index; its runner-up gap is
-//     certified against a coarse margin, else a fine int64 pass decides;
-//   * the exact d = 0 score (one lane), an integer-key merge with the step's
-//     pre-merged best over d >= 1 and the init rule, quantisation.
-// The helper warps (the rest of the CTA) prepare step t+1 meanwhile: worker
-// partials, window sums, the candidates d = 1..L-1 (which need only slots
-// <= t-1), and all global stores.  A named barrier hands the matvec result
-// (slot t-1) from the critical warps to the helpers inside the step.
+// The serial critical path of a step is: delta[t-1] final -> B[t-1][j] =
+// max_i(trans[j][i] + delta[t-1][i]) for every j -> the d = 0 candidate ->
+// merge -> delta[t].  Only that chain runs in the critical warps:
+//   * the matvec, 4 lanes per state, in packed int32: coarse score << 7 |
+//     (127 - i), so one integer max yields the value and the lowest index;
+//     its runner-up gap is certified against a coarse margin, else a fine
+//     int64 pass decides;
+//   * then one lane per state (the dense phase): the d = 0 candidate's
+//     fixed-point score W0 against Wtop, the best fixed-point score over
+//     d >= 1 that the helpers prepared one step ahead with the exact winner
+//     among d >= 1.  When W0 trails Wtop by more than the certified margin,
+//     delta[t] is that winner and no floating-point operation runs; otherwise
+//     the d = 0 score is computed exactly (two dependent FP64 adds) and
+//     compared.
+// FP64 instructions cost the same pipe time whatever the number of active
+// lanes, so exact scores are computed one lane per state, never one lane in
+// four.
+// The helper warps (the rest of the CTA) prepare step t+1 meanwhile: intake
+// of the workers' partial winners (loaded a step ahead), window sums (copied
+// asynchronously three steps ahead from a table built before the launch),
+// the candidates d = 1..L-1 in fixed point, certification, and in a dense
+// phase the exact score of the winner when it is one of them; also all global
+// stores.  A named barrier hands the matvec result (slot t-1) from the
+// critical warps to the helpers inside the step.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void cs_arrive() {
-  asm volatile("bar.arrive 2, %0;" ::"r"(GRID_THREADS) : "memory");
+constexpr int HWR = 4;  // rows of window sums kept by the head: steps t .. t+3
+
+// Named barriers of the head CTA (the CTA-wide barrier 0 is used only while
+// every thread is alive; threads without a role leave before the steps).
+// Non-aligned forms: they count threads, so a warp whose lanes took different
+// branches may arrive lane by lane.
+enum { BAR_STEP = 1, BAR_SLOT = 2, BAR_DENSE = 3, BAR_PW = 4 };
+__device__ __forceinline__ void named_sync(int id, int count) {
+  asm volatile("barrier.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
-__device__ __forceinline__ void helper_wait_cs() {
-  asm volatile("bar.sync 2, %0;" ::"r"(GRID_THREADS) : "memory");
+__device__ __forceinline__ void named_arrive(int id, int count) {
+  asm volatile("barrier.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
+
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all_but_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 __device__ __forceinline__ int coarse_of(long long fine_minus_base, int sh) {
   long long v = fine_minus_base >> sh;  // arithmetic shift: floor
@@ -456,6 +551,29 @@ __device__ __forceinline__ void packed_push(int p, int& b1, int& b2) {
   b2 = max(b2, lo);
 }
 
+__device__ __forceinline__ void group_reduce_exact(ExactBest& eb, unsigned gmask) {
+#pragma unroll
+  for (int o = HEAD_GROUP / 2; o > 0; o >>= 1) {
+    const long long ok = __shfl_xor_sync(gmask, eb.k, o);
+    const int od = __shfl_xor_sync(gmask, eb.d, o);
+    const int oi = __shfl_xor_sync(gmask, eb.i, o);
+    eb.offer_key(ok, od, oi);
+  }
+}
+
+// A worker segment's exact winner, kept as its order key and its fixed-point
+// value (the value of the segment's best candidate, to within half a unit).
+__device__ __forceinline__ void take_partial(const TaggedMsg& pm, int k, int qf, long long* pwq, long long* pwk,
+                                             int* pwd, int* pwi) {
+  double v;
+  int d, i;
+  msg_unpack(pm, v, d, i);
+  pwq[k] = d != EMPTY_D ? fixed_from_double(v, qf) : 0;
+  pwk[k] = order_key(v);
+  pwd[k] = d;
+  pwi[k] = i;
+}
+
 __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBufs& B, unsigned char* sm) {
   constexpr int L = GRID_L;
   constexpr int G4 = HEAD_GROUP;
@@ -463,36 +581,60 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const unsigned gmask = 0xfu << ((lane / G4) * G4);
   const long long T = B.T;
+  const long long margin = m.margin;
   int* Qcp = (int*)(sm + P.h_qcp);                    // [N][Np] packed coarse trans
   long long* qtr = (long long*)(sm + P.h_qtr);        // [N][N] fine trans
+  double* trh_s = (double*)(sm + P.h_trh);            // [N][N] exact trans (when it fits)
+  const double* trh = P.trans_smem ? trh_s : m.trans;
   int* dqcp = (int*)(sm + P.h_dqcp);                  // [2][Np] packed coarse delta
   long long* dq = (long long*)(sm + P.h_dq);          // [2][N] fine delta
-  long long* ptil = (long long*)(sm + P.h_ptil);      // [2][N] emission prefix P(t)
+  long long* ptil = (long long*)(sm + P.h_ptil);      // [4][N] emission prefix P(t), row t % 4
   long long* basebuf = (long long*)(sm + P.h_base);   // [2] coarse base per step
   double* dstar_h = (double*)(sm + P.h_dstar);        // [L+1][N] exact delta
   long long* ctil_h = (long long*)(sm + P.h_ctil);    // [L][N]
   unsigned short* itil_h = (unsigned short*)(sm + P.h_itil);
-  double* E = (double*)(sm + P.h_E);                  // [2][L][N] window sums of a step
+  double* hwr = (double*)(sm + P.h_hwr);              // [HWR][L][N] window sums, row t % HWR
   long long* qd_h = (long long*)(sm + P.h_qd);        // [N][L]
   double* dur_h = (double*)(sm + P.h_dur);            // [N][L]
-  long long* prek = (long long*)(sm + P.h_prek);      // [2][N] best over d >= 1: order key
+  long long* prek = (long long*)(sm + P.h_prek);      // [2][N] exact winner over d >= 1: order key
   int* pred = (int*)(sm + P.h_pred);
   int* prei = (int*)(sm + P.h_prei);
-  long long* pwk = (long long*)(sm + P.h_pwk);        // [S] worker partials of the next step
+  long long* prew = (long long*)(sm + P.h_prew);      // [2][N] best fixed-point score over d >= 1
+  long long* preq = (long long*)(sm + P.h_preq);      // [2][N] fixed-point value of the exact winner
+  long long* pwq = (long long*)(sm + P.h_pwq);        // [S] worker partials of the next step
+  long long* pwk = (long long*)(sm + P.h_pwk);
   int* pwd = (int*)(sm + P.h_pwd);
   int* pwi = (int*)(sm + P.h_pwi);
   uint32_t* psirec = (uint32_t*)(sm + P.h_psirec);    // [2][N] back-pointer word of a step
   double* tail = (double*)(sm + P.h_tail);
   __shared__ int s_fail;
   const int sh = P.coarse_shift;
-  const bool is_cs = tid < P.cs_threads;
-  const int hb = is_cs ? tid : tid - P.cs_threads;    // index within the role
-  const int gj = hb / G4, gl = hb % G4;                // state and lane of this group
-  const bool has_j = gj < N;
-  const int j = gj;
+  // Roles, by thread range:
+  //   [0, cs)             critical: the matvec, 4 lanes per state; the first
+  //                       cs_dense threads then run the dense phase, one lane per state
+  //   [cs, cs+st)         state helpers, one lane per state: step t+1's
+  //                       candidates, certification and exact winner, stores
+  //   [cs+st, cs+st+in)   intake of the workers' partial winners, one lane per
+  //                       segment; the first of these warps also computes the coarse base
+  // Threads beyond these leave once the tables are set up.
+  const int cs = P.cs_threads, st = P.st_threads, in = P.in_threads;
+  const int nthr = cs + st + in;
+  const bool is_cs = tid < cs;
+  const bool is_st = !is_cs && tid < cs + st;
+  const bool is_in = !is_cs && !is_st && tid < nthr;
+  const int gj = tid / G4, gl = tid % G4;              // critical: state and lane of this group
+  const int sj = tid - cs;                             // state helper: state
+  const int pk = tid - cs - st;                        // intake: segment
+  const bool has_sj = is_st && sj < N;
+  const bool has_pk = is_in && pk < S;
+  int k0 = 0, k1 = 0;
+  if (has_sj) {
+    k0 = B.seg_first[sj];
+    k1 = k0 + B.seg_count[sj];
+  }
 
-  // ---- initial state (t = 0) ----
-  for (int k = tid; k < N * Np; k += GRID_THREADS) {
+  // ---- initial state (t = 0), all threads ----
+  for (int k = tid; k < N * Np; k += blockDim.x) {
     const int jj = k / Np, i = k % Np;
     if (i < N) {
       const int c = coarse_of(m.qtr[(size_t)jj * N + i], sh);
@@ -501,22 +643,28 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
       Qcp[k] = INT_MIN;
     }
   }
-  for (int k = tid; k < N * N; k += GRID_THREADS) qtr[k] = m.qtr[k];
-  for (int k = tid; k < N * L; k += GRID_THREADS) {
+  for (int k = tid; k < N * N; k += blockDim.x) {
+    qtr[k] = m.qtr[k];
+    if (P.trans_smem) trh_s[k] = m.trans[k];
+  }
+  for (int k = tid; k < N * L; k += blockDim.x) {
     const int jj = k / L, d = k % L;
     qd_h[k] = m.qdurT[(size_t)jj * D + d];
     dur_h[k] = m.durT[(size_t)jj * D + d];
   }
-  for (int k = tid; k < 2 * Np; k += GRID_THREADS) dqcp[k] = 0;
-  for (int jj = tid; jj < N; jj += GRID_THREADS) {
+  for (int k = tid; k < 2 * Np; k += blockDim.x) dqcp[k] = 0;
+  for (int jj = tid; jj < N; jj += blockDim.x) {
     const double d0 = B.dinit[jj];
     dstar_h[jj] = d0;
     tagged64_store(B.dstar + (size_t)jj * 2, 1u, (unsigned long long)__double_as_longlong(d0));
-    dq[jj] = quantize(d0, m.scale);
-    ptil[jj] = m.qem[(size_t)B.obs[0] * N + jj];  // P(0)
+    dq[jj] = fixed_from_double(d0, P.qf);
+    const long long p0 = m.qem[(size_t)B.obs[0] * N + jj];
+    ptil[jj] = p0;                                                        // P(0)
+    if (T > 1) ptil[N + jj] = p0 + m.qem[(size_t)B.obs[1] * N + jj];  // P(1)
     B.psi[jj] = pack_psi(0, 0);
-    if (T > 1) E[(1 & 1) * L * N + jj] = m.em[(size_t)B.obs[1] * N + jj];  // E_1[0]
   }
+  for (int k = tid; k < HWR * L * N; k += blockDim.x)  // window sums of steps 0..3
+    if (k / (L * N) < T) hwr[k] = B.hwin[k];
   if (tid == 0) s_fail = 0;
   __syncthreads();
   if (warp == 0) {
@@ -527,35 +675,53 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
     if (lane == 0) { basebuf[0] = mx; basebuf[1] = mx; }
   }
   __syncthreads();
-  for (int jj = tid; jj < N; jj += GRID_THREADS) dqcp[jj] = coarse_of(dq[jj] - basebuf[0], sh) * 128;
-  // pre-merged best over d >= 1 for step 1: only the workers' (empty) partials
-  if (tid < S) {
-    TaggedMsg pm;
-    msg_load(B.part + ((size_t)(1 & (PART_RING - 1)) * S + tid) * 3, pm);
-    if (T > 1 && !msg_wait(B.part + ((size_t)(1 & (PART_RING - 1)) * S + tid) * 3, 1u, pm, B.abort_flag, P.timeout)) {
+  for (int jj = tid; jj < N; jj += blockDim.x) dqcp[jj] = coarse_of(dq[jj] - basebuf[0], sh) * 128;
+  // worker partials of step 1 (all empty: no d >= L yet), and the prefetch of step 2
+  TaggedMsg pm;
+  if (has_pk && T > 1) {
+    const unsigned long long* src = B.part + ((size_t)(1 & (PART_RING - 1)) * S + pk) * MSG_WORDS;
+    msg_load(src, pm);
+    if (!msg_wait(src, 1u, pm, B.abort_flag, P.timeout)) {
       grid_fail(B, TV_ETIMEOUT_DEV, SITE_HEAD_PARTIAL);
       s_fail = 1;
     } else {
-      double v;
-      msg_unpack(pm, v, pwd[tid], pwi[tid]);
-      pwk[tid] = order_key(v);
+      take_partial(pm, pk, P.qf, pwq, pwk, pwd, pwi);
     }
+    if (T > 2) msg_load(B.part + ((size_t)(2 & (PART_RING - 1)) * S + pk) * MSG_WORDS, pm);
   }
   __syncthreads();
   if (s_fail) return;
-  for (int jj = tid; jj < N; jj += GRID_THREADS) {
+  for (int jj = tid; jj < N; jj += blockDim.x) {
+    const int a = B.seg_first[jj], b = a + B.seg_count[jj];
+    const long long p1 = ptil[N + jj];
+    long long W = QNEG;
+    for (int k = a; k < b; ++k)
+      if (pwd[k] != EMPTY_D) W = max(W, pwq[k] - p1);
     ExactBest eb;
     eb.init();
-    const int k0 = B.seg_first[jj], k1 = k0 + B.seg_count[jj];
-    for (int k = k0; k < k1; ++k)
-      if (pwd[k] != EMPTY_D) eb.offer_key(pwk[k], pwd[k], pwi[k]);
+    for (int k = a; k < b; ++k)
+      if (pwd[k] != EMPTY_D && pwq[k] - p1 >= W - margin) eb.offer_key(pwk[k], pwd[k], pwi[k]);
+    prew[(1 & 1) * N + jj] = W;
     prek[(1 & 1) * N + jj] = eb.k;
     pred[(1 & 1) * N + jj] = eb.d;
     prei[(1 & 1) * N + jj] = eb.i;
+    preq[(1 & 1) * N + jj] = eb.d != IDX_NONE ? fixed_from_double(eb.value(), P.qf) : 0;
   }
-  double di_cur = 0.0;
-  if (is_cs && has_j && gl == 0 && 1 < D) di_cur = __ldcg(B.dinit + (size_t)1 * N + j);
   __syncthreads();
+  if (tid >= nthr) return;  // no role in the steps
+
+  // Register pipelines: a state helper keeps the prefix term of step t+2 and
+  // the observation of step t+3; an intake lane the partial message of step
+  // t+2 (in pm); a dense critical lane the initialisation score of step t+1.
+  long long qe_pf = 0;
+  int ob_q = 0;
+  if (has_sj) {
+    if (2 < T) qe_pf = m.qem[(size_t)B.obs[2] * N + sj];
+    if (3 < T) ob_q = B.obs[3];
+  }
+  double di_cur = 0.0;  // initialisation score of step t, state tid (dense critical lanes)
+  if (tid < N && 1 < D) di_cur = __ldcg(B.dinit + (size_t)1 * N + tid);
+  const int hw_chunks = L * N / 2;  // 16-byte pieces of a window-sum row
 
   int drow_prev = 0;  // (t-1) % (L+1): row of delta[t-1] in dstar_h
   int rdrow = 1;      // t % Rd: row of delta[t] in the tagged ring
@@ -563,14 +729,15 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
     const int cur = (int)(t & 1), prv = cur ^ 1;
     const int drow = drow_prev + 1 == L + 1 ? 0 : drow_prev + 1;  // t % (L+1)
     const int hrow = (int)((t - 1) & (L - 1));                      // slot t-1 in ctil_h
+    const long long t1 = t + 1;
+    const bool next = t1 < T;
+    const int nxt = cur ^ 1;  // (t+1) & 1
     if (is_cs) {
       // ================= critical warps =================
       double di_next = 0.0;
-      if (has_j && gl == 0 && t + 1 < D) di_next = __ldcg(B.dinit + (size_t)(t + 1) * N + j);
-      int ifine = 0;
-      bool amb = false;
-      long long bfine = 0;
-      if (has_j) {
+      if (tid < N && t + 1 < D) di_next = __ldcg(B.dinit + (size_t)(t + 1) * N + tid);
+      if (gj < N) {
+        const int j = gj;
         // packed coarse matvec over i for slot t-1
         int b1 = INT_MIN, b2 = INT_MIN;
         const int* qrow = Qcp + j * Np;
@@ -591,8 +758,9 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
           b1 = max(b1, o1);
           b2 = max(max(b2, o2), lo);
         }
-        ifine = 127 - (b1 & 127);
-        amb = ((b1 >> 7) - (b2 >> 7)) <= P.coarse_margin;
+        int ifine = 127 - (b1 & 127);
+        bool amb = ((b1 >> 7) - (b2 >> 7)) <= P.coarse_margin;
+        long long bfine;
         if (!amb) {
           bfine = qtr[j * N + ifine] + dq[prv * N + ifine];
         } else {
@@ -609,196 +777,218 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
           }
           ifine = tb.x1;
           bfine = tb.b1;
-          amb = (tb.b1 - tb.b2) <= m.margin;
+          amb = (tb.b1 - tb.b2) <= margin;
         }
         if (gl == 0) {
-          ctil_h[hrow * N + j] = bfine - ptil[prv * N + j];
+          ctil_h[hrow * N + j] = bfine - ptil[(int)((t - 1) & 3) * N + j];
           itil_h[hrow * N + j] = (unsigned short)(ifine | (amb ? 0x8000 : 0));
         }
       }
-      cs_arrive();  // slot t-1 ready for the helpers
-      if (has_j) {
-        // the d = 0 candidate, exact (src/hsmm.cu:341-346 with E_t[0] = em_t)
-        ExactBest eb;
-        eb.init();
-        const double e0 = E[cur * L * N + j];
-        if (!amb) {
-          if (gl == 0)
-            eb.set((e0 + dstar_h[drow_prev * N + ifine]) + (m.trans[(size_t)j * N + ifine] + dur_h[j * L]), 0,
-                   ifine);
-        } else {
-          const double* row = dstar_h + drow_prev * N;
-          const double* trj = m.trans + (size_t)j * N;
-          for (int i = gl; i < N; i += G4) eb.offer((e0 + row[i]) + (trj[i] + dur_h[j * L]), 0, i);
-#pragma unroll
-          for (int o = G4 / 2; o > 0; o >>= 1) {
-            const long long ok = __shfl_xor_sync(gmask, eb.k, o);
-            const int od = __shfl_xor_sync(gmask, eb.d, o);
-            const int oi = __shfl_xor_sync(gmask, eb.i, o);
-            eb.offer_key(ok, od, oi);
+      named_arrive(BAR_SLOT, cs + st);  // slot t-1 ready for the state helpers
+      if (tid < P.cs_dense) {
+        named_sync(BAR_DENSE, cs);
+        if (tid < N) {
+          // dense phase, one lane per state; the exact d = 0 score of the
+          // certified argmax over i is computed before it is known to be needed
+          const int dj = tid;
+          const long long W0 = ctil_h[hrow * N + dj] + qd_h[dj * L];  // the d = 0 candidate, fixed point
+          const unsigned short it = itil_h[hrow * N + dj];
+          const long long Wt = prew[cur * N + dj];
+          const long long pk0 = prek[cur * N + dj];
+          const int pd0 = pred[cur * N + dj], pi0 = prei[cur * N + dj];
+          const long long pq0 = preq[cur * N + dj];
+          const int i1 = it & 0x7fff;
+          const double e0 = hwr[(int)(t & (HWR - 1)) * L * N + dj];
+          const double du0 = dur_h[dj * L];
+          // src/hsmm.cu:341-346 with E_t[0]
+          const double V0 = (e0 + dstar_h[drow_prev * N + i1]) + (trh[(size_t)dj * N + i1] + du0);
+          const long long q0 = fixed_from_double(V0, P.qf);
+          long long kk = pk0, fq = pq0;
+          int dd = pd0, ii = pi0;
+          if (W0 >= Wt - margin) {
+            ExactBest eb;
+            if (!(it & 0x8000)) {
+              eb.set(V0, 0, i1);
+            } else {
+              eb.init();
+              const double* row = dstar_h + drow_prev * N;
+              const double* trj = trh + (size_t)dj * N;
+              for (int i = 0; i < N; ++i) eb.offer((e0 + row[i]) + (trj[i] + du0), 0, i);
+            }
+            if (W0 <= Wt + margin) eb.offer_key(pk0, pd0, pi0);
+            kk = eb.k;
+            dd = eb.d;
+            ii = eb.i;
+            if (dd == 0) fq = (it & 0x8000) ? fixed_from_double(eb.value(), P.qf) : q0;
           }
-        }
-        if (gl == 0) {
-          eb.offer_key(prek[cur * N + j], pred[cur * N + j], prei[cur * N + j]);
-          double fin;
-          uint32_t wv;
+          double fin = key_value(kk);
+          uint32_t wv = pack_psi(dd, ii);
           // t < D: the induction result replaces the initialisation score only
           // when strictly larger (src/hsmm.cu:353-358).
-          if (t >= D || eb.k > order_key(di_cur)) {
-            fin = eb.value();
-            wv = pack_psi(eb.d, eb.i);
-          } else {
+          if (t < D && !(kk > order_key(di_cur))) {
             fin = di_cur;
             wv = pack_psi((int)t, 0);
+            fq = fixed_from_double(fin, P.qf);
           }
-          dstar_h[drow * N + j] = fin;
-          const long long fq = quantize(fin, m.scale);
-          dq[cur * N + j] = fq;
-          dqcp[cur * Np + j] = coarse_of(fq - basebuf[cur], sh) * 128;
-          psirec[cur * N + j] = wv;
+          dstar_h[drow * N + dj] = fin;
+          dq[cur * N + dj] = fq;
+          dqcp[cur * Np + dj] = coarse_of(fq - basebuf[cur], sh) * 128;
+          psirec[cur * N + dj] = wv;
         }
+      } else {
+        named_arrive(BAR_DENSE, cs);
       }
       di_cur = di_next;
+    } else if (is_st) {
+      // ============ state helpers: prepare step t+1, one lane per state ============
+      // window sums of step t+3 into the ring; the copies of step t+2 are
+      // complete before this step's closing barrier
+      for (int c = sj; c < hw_chunks; c += st)
+        if (t + 3 < T)
+          cp_async16(hwr + (int)((t + 3) & (HWR - 1)) * L * N + c * 2, B.hwin + (size_t)(t + 3) * L * N + c * 2);
+      cp_async_commit();
+      cp_async_wait_all_but_1();
+      if (has_sj) {
+        if (next) {
+          ptil[(int)(t1 & 3) * N + sj] = ptil[(int)(t & 3) * N + sj] + qe_pf;  // P(t+1)
+          if (t + 2 < T) qe_pf = m.qem[(size_t)ob_q * N + sj];
+          if (t + 3 < T) ob_q = B.obs[t + 3];
+        }
+        // results of step t-1 to global memory
+        if (t >= 2) {
+          B.psi[(size_t)(t - 1) * N + sj] = psirec[prv * N + sj];
+          tagged64_store(B.dstar + ((size_t)(rdrow == 0 ? P.Rd - 1 : rdrow - 1) * N + sj) * 2, (unsigned)t,
+                         (unsigned long long)__double_as_longlong(dstar_h[drow_prev * N + sj]));
+        }
+      }
+      named_sync(BAR_SLOT, cs + st);  // the critical warps published slot t-1
+      if (has_sj) {
+        // slot t-1 message for the workers
+        unsigned long long* msg =
+            B.slot_msg + ((size_t)((unsigned)(t - 1) & (SLOT_RING - 1)) * N + sj) * SLOT_WORDS;
+        const unsigned tag = (unsigned)t;
+        const unsigned short itv = itil_h[hrow * N + sj];
+        tagged64_store(msg, tag, (unsigned long long)ctil_h[hrow * N + sj]);
+        tagged64_store(msg + 2, tag,
+                       (unsigned long long)__double_as_longlong(dstar_h[drow_prev * N + (itv & 0x7fff)]));
+        st_relaxed_u64(msg + 4, ((unsigned long long)tag << 32) | itv);
+      }
+      named_sync(BAR_PW, st + in);  // the intake lanes took in the partials of step t+1
+      if (has_sj && next) {
+        // Every candidate d >= 1 of step t+1 in fixed point: d = 1..L-1 here
+        // (slots t-d), d >= L as the workers' winners, whose fixed-point
+        // scores are their values minus the prefix P(t+1).  Written for
+        // instruction-level parallelism: one lane carries a state, so its
+        // loads are issued together and the exact score of the best short
+        // candidate is computed before it is known to be needed.
+        const int tau1 = (int)(t1 < D ? t1 : D);
+        const int hl1 = tau1 < L ? tau1 : L;
+        const long long p1 = ptil[(int)(t1 & 3) * N + sj];
+        long long Wd[L];
+        unsigned short itd[L];
+#pragma unroll
+        for (int d = 1; d < L; ++d) {
+          const int row = (int)((t - d) & (L - 1));
+          Wd[d] = d < hl1 ? ctil_h[row * N + sj] + qd_h[sj * L + d] : QNEG;
+          itd[d] = itil_h[row * N + sj];
+        }
+        long long Wh = QNEG;
+        int dh = 0, ih = 0, hamb = 0;
+#pragma unroll
+        for (int d = 1; d < L; ++d)
+          if (Wd[d] > Wh) {
+            Wh = Wd[d];
+            dh = d;
+            ih = itd[d] & 0x7fff;
+            hamb = itd[d] & 0x8000;
+          }
+        double Vh = 0.0;
+        long long qh = 0;
+        if (dh > 0) {
+          int dr = drow_prev + 1 - dh;  // row of delta[t-dh]
+          if (dr < 0) dr += L + 1;
+          const double e = hwr[((int)(t1 & (HWR - 1)) * L + dh) * N + sj];
+          Vh = (e + dstar_h[dr * N + ih]) + (trh[(size_t)sj * N + ih] + dur_h[sj * L + dh]);
+          qh = fixed_from_double(Vh, P.qf);
+        }
+        long long Wl = Wh;
+        for (int k = k0; k < k1; ++k)
+          if (pwd[k] != EMPTY_D) Wl = max(Wl, pwq[k] - p1);
+        const long long thr = Wl - margin;
+        // exact winner among the candidates within the margin of the best,
+        // with its fixed-point value
+        ExactBest eb;
+        eb.init();
+        long long qb = 0;
+        for (int k = k0; k < k1; ++k)
+          if (pwd[k] != EMPTY_D && pwq[k] - p1 >= thr && eb.better_key(pwk[k], pwd[k], pwi[k])) {
+            eb.k = pwk[k];
+            eb.d = pwd[k];
+            eb.i = pwi[k];
+            qb = pwq[k];
+          }
+        int nh = 0;
+#pragma unroll
+        for (int d = 1; d < L; ++d) nh += Wd[d] >= thr ? 1 : 0;
+        if (nh == 1 && !hamb) {
+          const long long kh = order_key(Vh);
+          if (eb.better_key(kh, dh, ih)) {
+            eb.k = kh;
+            eb.d = dh;
+            eb.i = ih;
+            qb = qh;
+          }
+        } else if (nh > 0) {
+          // several short candidates in the margin, or an ambiguous argmax over i
+          for (int d = 1; d < hl1; ++d) {
+            if (Wd[d] < thr) continue;
+            const double e = hwr[((int)(t1 & (HWR - 1)) * L + d) * N + sj];
+            const double du = dur_h[sj * L + d];
+            int dr = drow_prev + 1 - d;  // row of delta[t-d]
+            if (dr < 0) dr += L + 1;
+            const double* drw = dstar_h + dr * N;
+            const double* trj = trh + (size_t)sj * N;
+            const unsigned short it = itd[d];
+            if (!(it & 0x8000)) {
+              const int i1 = it & 0x7fff;
+              eb.offer((e + drw[i1]) + (trj[i1] + du), d, i1);
+            } else {
+              for (int i = 0; i < N; ++i) eb.offer((e + drw[i]) + (trj[i] + du), d, i);
+            }
+          }
+          qb = eb.d == IDX_NONE ? 0 : fixed_from_double(eb.value(), P.qf);
+        }
+        prew[nxt * N + sj] = Wl;
+        prek[nxt * N + sj] = eb.k;
+        pred[nxt * N + sj] = eb.d;
+        prei[nxt * N + sj] = eb.i;
+        preq[nxt * N + sj] = qb;
+      }
     } else {
-      // ================= helper warps: prepare step t+1 =================
-      const long long t1 = t + 1;
-      const bool next = t1 < T;
-      const int nxt = cur ^ 1;  // (t+1) & 1
-      // worker partials of step t+1
-      if (next && hb < S) {
-        TaggedMsg pm;
-        msg_load(B.part + ((size_t)((unsigned)t1 & (PART_RING - 1)) * S + hb) * 3, pm);
-        if (!msg_wait(B.part + ((size_t)((unsigned)t1 & (PART_RING - 1)) * S + hb) * 3, (unsigned)t1, pm,
+      // ============ intake: worker partials of step t+1, loaded during the previous step ============
+      if (has_pk && next) {
+        if (!msg_wait(B.part + ((size_t)((unsigned)t1 & (PART_RING - 1)) * S + pk) * MSG_WORDS, (unsigned)t1, pm,
                       B.abort_flag, P.timeout)) {
           grid_fail(B, TV_ETIMEOUT_DEV, SITE_HEAD_PARTIAL);
           s_fail = 1;
         } else {
-          double v;
-          msg_unpack(pm, v, pwd[hb], pwi[hb]);
-          pwk[hb] = order_key(v);
+          take_partial(pm, pk, P.qf, pwq, pwk, pwd, pwi);
         }
+        if (t1 + 1 < T) msg_load(B.part + ((size_t)((unsigned)(t1 + 1) & (PART_RING - 1)) * S + pk) * MSG_WORDS, pm);
       }
-      if (has_j) {
-        // window sums of step t+1
-        if (next) {
-          const int ot1 = B.obs[t1];
-          const double em1 = m.em[(size_t)ot1 * N + j];
-          if (t1 > D) {
-            // E_{t+1}[d] = E_t[d-1] + em_{t+1}, E_{t+1}[0] = 0 + em_{t+1} (src/hsmm.cu:298-310)
-            for (int d = gl; d < L; d += G4) {
-              if (d == 0) {
-                const long long b = __double_as_longlong(em1);
-                E[nxt * L * N + j] = __longlong_as_double(b == (long long)0x8000000000000000ULL ? 0 : b);
-              } else {
-                E[(nxt * L + d) * N + j] = E[(cur * L + d - 1) * N + j] + em1;
-              }
-            }
-          } else if (gl == 0) {
-            // newest-first rebuild (src/hsmm.cu:311-322)
-            const int hl1 = (int)(t1 < L ? t1 : L);
-            double g = em1;
-            E[nxt * L * N + j] = g;
-            for (int d = 1; d < hl1; ++d) {
-              g = g + m.em[(size_t)B.obs[t1 - d] * N + j];
-              E[(nxt * L + d) * N + j] = g;
-            }
-          }
-        }
-        if (gl == 1) ptil[cur * N + j] = ptil[prv * N + j] + m.qem[(size_t)B.obs[t] * N + j];  // P(t)
-        // results of step t-1 to global memory
-        if (t >= 2) {
-          if (gl == 2) B.psi[(size_t)(t - 1) * N + j] = psirec[prv * N + j];
-          if (gl == 3)
-            tagged64_store(B.dstar + ((size_t)(rdrow == 0 ? P.Rd - 1 : rdrow - 1) * N + j) * 2, (unsigned)t,
-                           (unsigned long long)__double_as_longlong(dstar_h[drow_prev * N + j]));
-        }
-      }
-      // coarse base of step t+1: max_i delta[t-1] (the last helper warp)
-      if (hb >= GRID_THREADS - P.cs_threads - 32) {
-        const int l = hb - (GRID_THREADS - P.cs_threads - 32);
+      named_arrive(BAR_PW, st + in);
+      // coarse base of step t+1: max_i delta[t-1] (the first intake warp)
+      if (pk < 32) {
         long long mx = LLONG_MIN;
-        for (int i = l; i < N; i += 32) mx = max(mx, dq[prv * N + i]);
+        for (int i = pk; i < N; i += 32) mx = max(mx, dq[prv * N + i]);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (l == 0) basebuf[nxt] = mx;
-      }
-      helper_wait_cs();  // the critical warps published slot t-1
-      if (has_j) {
-        // slot t-1 message for the workers
-        unsigned long long* msg =
-            B.slot_msg + ((size_t)((unsigned)(t - 1) & (SLOT_RING - 1)) * N + j) * SLOT_WORDS;
-        const unsigned tag = (unsigned)t;
-        const unsigned short itv = itil_h[hrow * N + j];
-        if (gl == 0) tagged64_store(msg, tag, (unsigned long long)ctil_h[hrow * N + j]);
-        if (gl == 1)
-          tagged64_store(msg + 2, tag,
-                         (unsigned long long)__double_as_longlong(dstar_h[drow_prev * N + (itv & 0x7fff)]));
-        if (gl == 2) st_relaxed_u64(msg + 4, ((unsigned long long)tag << 32) | itv);
-        if (next) {
-          // candidates d = 1..L-1 of step t+1 (slots t-d), certified, exact
-          const int tau1 = (int)(t1 < D ? t1 : D);
-          const int hl1 = tau1 < L ? tau1 : L;
-          Top2 tb;
-          tb.init();
-          for (int dme = gl + 1; dme < hl1; dme += G4)
-            tb.push(ctil_h[((int)((t - dme) & (L - 1))) * N + j] + qd_h[j * L + dme], dme);
-#pragma unroll
-          for (int o = G4 / 2; o > 0; o >>= 1) {
-            const long long ob1 = __shfl_xor_sync(gmask, tb.b1, o);
-            const long long ob2 = __shfl_xor_sync(gmask, tb.b2, o);
-            const int ox1 = __shfl_xor_sync(gmask, tb.x1, o);
-            tb.merge(ob1, ox1, ob2);
-          }
-          ExactBest eb;
-          eb.init();
-          if (tb.x1 != IDX_NONE) {
-            const int d1 = tb.x1;
-            const unsigned short it = itil_h[((int)((t - d1) & (L - 1))) * N + j];
-            const bool amb = (it & 0x8000) || ((tb.b1 - tb.b2) <= m.margin);
-            if (!amb) {
-              if (gl == 0) {
-                const int i1 = it & 0x7fff;
-                int dr = drow_prev + 1 - d1;  // row of delta[t-d1]
-                if (dr < 0) dr += L + 1;
-                eb.set((E[(nxt * L + d1) * N + j] + dstar_h[dr * N + i1]) +
-                           (m.trans[(size_t)j * N + i1] + dur_h[j * L + d1]),
-                       d1, i1);
-              }
-            } else {
-              const long long thr = tb.b1 - m.margin;
-              for (int dme = gl + 1; dme < hl1; dme += G4) {
-                if (ctil_h[((int)((t - dme) & (L - 1))) * N + j] + qd_h[j * L + dme] < thr) continue;
-                const double e = E[(nxt * L + dme) * N + j];
-                const double du = dur_h[j * L + dme];
-                int dr = drow_prev + 1 - dme;
-                if (dr < 0) dr += L + 1;
-                const double* row = dstar_h + dr * N;
-                const double* trj = m.trans + (size_t)j * N;
-                for (int i = 0; i < N; ++i) eb.offer((e + row[i]) + (trj[i] + du), dme, i);
-              }
-#pragma unroll
-              for (int o = G4 / 2; o > 0; o >>= 1) {
-                const long long ok = __shfl_xor_sync(gmask, eb.k, o);
-                const int od = __shfl_xor_sync(gmask, eb.d, o);
-                const int oi = __shfl_xor_sync(gmask, eb.i, o);
-                eb.offer_key(ok, od, oi);
-              }
-            }
-          }
-          if (gl == 0) {
-            const int k0 = B.seg_first[j], k1 = k0 + B.seg_count[j];
-            for (int k = k0; k < k1; ++k)
-              if (pwd[k] != EMPTY_D) eb.offer_key(pwk[k], pwd[k], pwi[k]);
-            prek[nxt * N + j] = eb.k;
-            pred[nxt * N + j] = eb.d;
-            prei[nxt * N + j] = eb.i;
-          }
-        }
+        if (pk == 0) basebuf[nxt] = mx;
       }
     }
     drow_prev = drow;
     rdrow = rdrow + 1 == P.Rd ? 0 : rdrow + 1;
-    __syncthreads();
+    named_sync(BAR_STEP, nthr);
     if (s_fail) return;
   }
 
@@ -807,52 +997,43 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
     const long long t = T - 1;
     const int tau = (int)(t < D ? t : D);
     const int hl = tau < L ? tau : L;
-    if (tid < S) {
-      TaggedMsg pm;
-      msg_load(B.part + ((size_t)((unsigned)T & (PART_RING - 1)) * S + tid) * 3, pm);
-      if (!msg_wait(B.part + ((size_t)((unsigned)T & (PART_RING - 1)) * S + tid) * 3, (unsigned)T, pm, B.abort_flag,
-                    P.timeout)) {
+    if (has_pk) {
+      const unsigned long long* src = B.part + ((size_t)((unsigned)T & (PART_RING - 1)) * S + pk) * MSG_WORDS;
+      msg_load(src, pm);
+      if (!msg_wait(src, (unsigned)T, pm, B.abort_flag, P.timeout)) {
         grid_fail(B, TV_ETIMEOUT_DEV, SITE_HEAD_TAIL);
         s_fail = 1;
       } else {
-        double v;
-        msg_unpack(pm, v, pwd[tid], pwi[tid]);
-        pwk[tid] = order_key(v);
+        take_partial(pm, pk, P.qf, pwq, pwk, pwd, pwi);
       }
     }
-    __syncthreads();
+    named_sync(BAR_STEP, nthr);
     if (s_fail) return;
-    if (is_cs && has_j) {
+    if (is_cs && gj < N) {
+      const int j = gj;
       ExactBest eb;
       eb.init();
-      const int ec = (int)(t & 1);
       for (int d = gl; d < hl; d += G4) {
-        const double e = E[(ec * L + d) * N + j] + m.survT[(size_t)j * D + d];
+        const double e = hwr[((int)(t & (HWR - 1)) * L + d) * N + j] + m.survT[(size_t)j * D + d];
         // after the loop drow_prev is the row of delta[T-1]; the tail reads
         // delta[t-1-d] = delta[T-2-d]
         int dr = drow_prev - 1 - d;
         while (dr < 0) dr += L + 1;
         const double* row = dstar_h + dr * N;
-        const double* trj = m.trans + (size_t)j * N;
+        const double* trj = trh + (size_t)j * N;
         for (int i = 0; i < N; ++i) eb.offer((e + row[i]) + trj[i], d, i);
       }
-#pragma unroll
-      for (int o = G4 / 2; o > 0; o >>= 1) {
-        const long long ok = __shfl_xor_sync(gmask, eb.k, o);
-        const int od = __shfl_xor_sync(gmask, eb.d, o);
-        const int oi = __shfl_xor_sync(gmask, eb.i, o);
-        eb.offer_key(ok, od, oi);
-      }
+      group_reduce_exact(eb, gmask);
       if (gl == 0) {
-        const int k0 = B.seg_first[j], k1 = k0 + B.seg_count[j];
-        for (int k = k0; k < k1; ++k)
+        const int a = B.seg_first[j], b = a + B.seg_count[j];
+        for (int k = a; k < b; ++k)
           if (pwd[k] != EMPTY_D) eb.offer_key(pwk[k], pwd[k], pwi[k]);
         if (eb.d == IDX_NONE) { eb.d = 0; eb.i = 0; }
         tail[j] = eb.value();
         B.psi[(size_t)t * N + j] = pack_psi(eb.d, eb.i);
       }
     }
-    __syncthreads();
+    named_sync(BAR_STEP, nthr);
   }
 
   // Backtrace (src/hsmm.cu:139-170).

@@ -119,7 +119,7 @@ struct tv_model_s {
   int sm_count = 0;
   // grid-kernel scratch (single long sequences)
   DevBuf<unsigned long long> msgs;  // slot messages, partial messages, exact delta ring
-  DevBuf<double> dinit, ck;
+  DevBuf<double> dinit, ck, hwin;
   DevBuf<long long> wrange;
   DevBuf<int> seg_first, seg_count, seg_base, gflags;
   int plan_key_N = -1, plan_key_D = -1, plan_key_G = -1;
@@ -355,32 +355,44 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, tv::GridParams& P, std::vec
   P.w_acc1 = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
   P.w_itil = o; o = tv::tv_align(o + (unsigned long long)chunk * 2);
   P.w_red = o;  o = tv::tv_align(o + (unsigned long long)std::max(max_seg * (tv::WORKER_THREADS / 32) * sizeof(tv::Top2), 32 * sizeof(tv::ExactBest)));
+  P.w_emw = o;  o = tv::tv_align(o + (unsigned long long)2 * max_seg * 8);
   P.w_bytes = o;
   o = 0;
   const int Np = (N + 15) / 16 * 16;
   P.Np = Np;
   P.cs_threads = (tv::HEAD_GROUP * N + 31) / 32 * 32;
-  if (tv::GRID_THREADS - P.cs_threads < tv::HEAD_GROUP * N || tv::GRID_THREADS - P.cs_threads < 32) return false;
+  P.cs_dense = (N + 31) / 32 * 32;
+  P.st_threads = (N + 31) / 32 * 32;
+  P.in_threads = (S + 31) / 32 * 32;
+  P.block = std::max(P.cs_threads + P.st_threads + P.in_threads, tv::WORKER_THREADS);
+  if (P.block > tv::GRID_THREADS) return false;
   P.h_qcp = o;    o = tv::tv_align(o + (unsigned long long)N * Np * 4);
   P.h_qtr = o;    o = tv::tv_align(o + (unsigned long long)N * N * 8);
   P.h_dqcp = o;   o = tv::tv_align(o + (unsigned long long)2 * Np * 4);
   P.h_dq = o;     o = tv::tv_align(o + (unsigned long long)2 * N * 8);
-  P.h_ptil = o;   o = tv::tv_align(o + (unsigned long long)2 * N * 8);
+  P.h_ptil = o;   o = tv::tv_align(o + (unsigned long long)4 * N * 8);
   P.h_base = o;   o = tv::tv_align(o + 16);
   P.h_dstar = o;  o = tv::tv_align(o + (unsigned long long)(L + 1) * N * 8);
   P.h_ctil = o;   o = tv::tv_align(o + (unsigned long long)L * N * 8);
   P.h_itil = o;   o = tv::tv_align(o + (unsigned long long)L * N * 2);
-  P.h_E = o;      o = tv::tv_align(o + (unsigned long long)2 * L * N * 8);
+  P.h_hwr = o;    o = tv::tv_align(o + (unsigned long long)tv::HWR * L * N * 8);
   P.h_qd = o;     o = tv::tv_align(o + (unsigned long long)N * L * 8);
   P.h_dur = o;    o = tv::tv_align(o + (unsigned long long)N * L * 8);
   P.h_prek = o;   o = tv::tv_align(o + (unsigned long long)2 * N * 8);
   P.h_pred = o;   o = tv::tv_align(o + (unsigned long long)2 * N * 4);
   P.h_prei = o;   o = tv::tv_align(o + (unsigned long long)2 * N * 4);
+  P.h_prew = o;   o = tv::tv_align(o + (unsigned long long)2 * N * 8);
+  P.h_preq = o;   o = tv::tv_align(o + (unsigned long long)2 * N * 8);
+  P.h_pwq = o;    o = tv::tv_align(o + (unsigned long long)S * 8);
   P.h_pwk = o;    o = tv::tv_align(o + (unsigned long long)S * 8);
   P.h_pwd = o;    o = tv::tv_align(o + (unsigned long long)S * 4);
   P.h_pwi = o;    o = tv::tv_align(o + (unsigned long long)S * 4);
   P.h_psirec = o; o = tv::tv_align(o + (unsigned long long)2 * N * 4);
   P.h_tail = o;   o = tv::tv_align(o + (unsigned long long)N * 8);
+  // the exact transition matrix joins the head's shared memory when it fits
+  P.h_trh = o;
+  P.trans_smem = o + (unsigned long long)N * N * 8 + 256 <= (unsigned long long)smem_optin ? 1 : 0;
+  if (P.trans_smem) o = tv::tv_align(o + (unsigned long long)N * N * 8);
   P.h_bytes = o;
   P.timeout = 1LL << 31;  // SM clock cycles, about a second: no legitimate wait comes close
   return std::max(P.w_bytes, P.h_bytes) + 256 <= (unsigned long long)smem_optin;
@@ -395,12 +407,13 @@ int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_
   if ((rc = prepare_quant(m, Q, st)) != TV_OK) return rc;
   if ((rc = m->psi.ensure((size_t)T * N)) != TV_OK) return rc;
   const size_t slot_words = (size_t)tv::SLOT_RING * N * tv::SLOT_WORDS;
-  const size_t part_words = (size_t)tv::PART_RING * P.S * 3;
+  const size_t part_words = (size_t)tv::PART_RING * P.S * tv::MSG_WORDS;
   const size_t dstar_words = (size_t)P.Rd * N * 2;
   if ((rc = m->msgs.ensure(slot_words + part_words + dstar_words)) != TV_OK) return rc;
   if ((rc = m->dinit.ensure((size_t)D * N)) != TV_OK) return rc;
   const int tmax = (int)std::min<int64_t>(D, T - 1);
   if ((rc = m->ck.ensure((size_t)std::max(tmax, 1) * P.M * N)) != TV_OK) return rc;
+  if ((rc = m->hwin.ensure((size_t)T * tv::GRID_L * N)) != TV_OK) return rc;
   if ((rc = m->gflags.ensure(4)) != TV_OK) return rc;
   // Tags start at 1: a cleared buffer holds no valid message.
   TV_CUDA(cudaMemsetAsync(m->msgs.p, 0, sizeof(unsigned long long) * (slot_words + part_words + dstar_words), st));
@@ -416,6 +429,11 @@ int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_
     tv::grid_prep_ck<<<(unsigned)((nthr + 255) / 256), 256, 0, st>>>(mv, obs_dev, m->ck.p, P.M, tmax, gabort);
     m->last_launches += 1;
   }
+  {
+    const long long nthr = T * N;
+    tv::grid_prep_hwin<<<(unsigned)((nthr + 255) / 256), 256, 0, st>>>(mv, obs_dev, T, m->hwin.p, gabort);
+    m->last_launches += 1;
+  }
   TV_CUDA(cudaGetLastError());
   tv::GridBufs B{};
   B.obs = obs_dev;
@@ -428,6 +446,7 @@ int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_
   B.dstar = m->msgs.p + slot_words + part_words;
   B.dinit = m->dinit.p;
   B.ck = m->ck.p;
+  B.hwin = m->hwin.p;
   B.wrange = m->wrange.p;
   B.seg_first = m->seg_first.p;
   B.seg_count = m->seg_count.p;
@@ -441,6 +460,7 @@ int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_
   // the exact value; a coarse runner-up gap above the margin certifies the
   // argmax over i.
   Pc.coarse_shift = Q.f - tv::COARSE_F;
+  Pc.qf = Q.f;
   {
     const double u = std::ldexp(1.0, -53), q = std::ldexp(1.0, -Q.f), qc = std::ldexp(1.0, -tv::COARSE_F);
     const double S_ = (double)T * (m->emax + m->tmax + m->dmax) + m->smax + (double)m->D * m->emax + m->tmax + m->dmax;
@@ -450,7 +470,7 @@ int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_
   const size_t dyn = std::max(P.w_bytes, P.h_bytes);
   TV_CUDA(cudaFuncSetAttribute(tv::grid_decode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
   mark_start(m, st);
-  TV_CUDA(cudaLaunchCooperativeKernel((void*)tv::grid_decode_kernel, dim3(P.G), dim3(tv::GRID_THREADS), args, dyn, st));
+  TV_CUDA(cudaLaunchCooperativeKernel((void*)tv::grid_decode_kernel, dim3(P.G), dim3(P.block), args, dyn, st));
   mark_end(m, st);
   m->last_launches += 1;
   return TV_OK;
@@ -485,7 +505,7 @@ int launch_single(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* pat
       } else {
         const size_t dyn = std::max(P.w_bytes, P.h_bytes);
         TV_CUDA(cudaFuncSetAttribute(tv::grid_decode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-        TV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tv::grid_decode_kernel, tv::GRID_THREADS, dyn));
+        TV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tv::grid_decode_kernel, P.block, dyn));
         if (per_sm < 1) return fail(TV_EINVAL, "grid kernel does not fit on an SM");
         int rc;
         if ((rc = m->seg_first.ensure(first.size())) != TV_OK) return rc;

@@ -35,8 +35,9 @@ __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned l
 // high half.  Single 8-byte stores are single-copy atomic, so a reader that
 // sees the expected tag in all three words holds a consistent message
 // without any fence: one L2 round trip per message.
+constexpr int MSG_WORDS = 3;
 struct TaggedMsg {
-  unsigned long long w[3];
+  unsigned long long w[MSG_WORDS];
 };
 
 __device__ __forceinline__ void msg_pack(TaggedMsg& m, unsigned tag, double v, int d, int i) {
