@@ -39,7 +39,7 @@
 
 namespace tv {
 
-constexpr int GRID_THREADS = 768;    // largest block: the head's roles for N <= 128
+constexpr int GRID_THREADS = 640;    // largest block: the head's roles (N up to about 96)
 constexpr int WORKER_THREADS = 256;  // a worker CTA keeps 8 warps; the rest exit at once
 constexpr int GRID_L = 8;            // head candidates d < L (a power of two)
 constexpr int CK_STRIDE = 32;      // checkpoint stride of the early window sums
@@ -802,7 +802,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
           const double du0 = dur_h[dj * L];
           // src/hsmm.cu:341-346 with E_t[0]
           const double V0 = (e0 + dstar_h[drow_prev * N + i1]) + (trh[(size_t)dj * N + i1] + du0);
-          const long long q0 = fixed_from_double(V0, P.qf);
+          const long long q0 = quantize(V0, m.scale);
           long long kk = pk0, fq = pq0;
           int dd = pd0, ii = pi0;
           if (W0 >= Wt - margin) {
@@ -819,7 +819,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
             kk = eb.k;
             dd = eb.d;
             ii = eb.i;
-            if (dd == 0) fq = (it & 0x8000) ? fixed_from_double(eb.value(), P.qf) : q0;
+            if (dd == 0) fq = (it & 0x8000) ? quantize(eb.value(), m.scale) : q0;
           }
           double fin = key_value(kk);
           uint32_t wv = pack_psi(dd, ii);
@@ -828,7 +828,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
           if (t < D && !(kk > order_key(di_cur))) {
             fin = di_cur;
             wv = pack_psi((int)t, 0);
-            fq = fixed_from_double(fin, P.qf);
+            fq = quantize(fin, m.scale);
           }
           dstar_h[drow * N + dj] = fin;
           dq[cur * N + dj] = fq;
@@ -909,7 +909,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
           if (dr < 0) dr += L + 1;
           const double e = hwr[((int)(t1 & (HWR - 1)) * L + dh) * N + sj];
           Vh = (e + dstar_h[dr * N + ih]) + (trh[(size_t)sj * N + ih] + dur_h[sj * L + dh]);
-          qh = fixed_from_double(Vh, P.qf);
+          qh = quantize(Vh, m.scale);
         }
         long long Wl = Wh;
         for (int k = k0; k < k1; ++k)
@@ -956,7 +956,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
               for (int i = 0; i < N; ++i) eb.offer((e + drw[i]) + (trj[i] + du), d, i);
             }
           }
-          qb = eb.d == IDX_NONE ? 0 : fixed_from_double(eb.value(), P.qf);
+          qb = eb.d == IDX_NONE ? 0 : quantize(eb.value(), m.scale);
         }
         prew[nxt * N + sj] = Wl;
         prek[nxt * N + sj] = eb.k;
