@@ -49,6 +49,7 @@ WORKLOADS = {
     "single_N75_D5000_T1e6": dict(N=75, D=5000, T=1_000_000, M=32, lo=50.0, hi=2500.0, seed=1),
     "single_N10_D100_T1e3": dict(N=10, D=100, T=1000, M=16, lo=5.0, hi=50.0, seed=0),
     "single_N100_D10000_T1e6": dict(N=100, D=10_000, T=1_000_000, M=64, lo=5.0, hi=50.0, seed=4),
+    "single_N100_D10000_T1e7": dict(N=100, D=10_000, T=10_000_000, M=64, lo=5.0, hi=50.0, seed=4),
     # 4096 sequences sharing one model, lengths log-uniform in [1e3, 1e5]
     "batch_4096_N10_D250": dict(kind="batch", n_seq=4096, N=10, D=250, M=16, lo=1e3, hi=1e5, seed=2),
 }

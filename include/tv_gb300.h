@@ -105,10 +105,12 @@ int64_t tv_model_last_launches(tv_model m);
 /* Kernel selection for single-sequence decodes (no reference counterpart):
  * TV_PATH_AUTO picks the one-CTA kernel when the D-deep window fits one
  * CTA's shared memory and the whole-GPU grid kernel otherwise;
- * TV_PATH_CTA / TV_PATH_GRID force one of them.  grid_ctas > 0 caps the
- * grid kernel's CTA count (0 = one per SM).  Both kernels give identical
+ * TV_PATH_CTA / TV_PATH_GRID force one of them.  The grid kernel keeps the
+ * window in its workers' shared memory, or in global memory (L2) when it
+ * does not fit there; TV_PATH_GRID_L2 forces the latter.  grid_ctas > 0
+ * caps the grid kernel's CTA count (0 = one per SM).  All give identical
  * results. */
-enum tv_path { TV_PATH_AUTO = 0, TV_PATH_CTA = 1, TV_PATH_GRID = 2 };
+enum tv_path { TV_PATH_AUTO = 0, TV_PATH_CTA = 1, TV_PATH_GRID = 2, TV_PATH_GRID_L2 = 3 };
 int tv_model_set_path(tv_model m, int path, int grid_ctas);
 
 /* Which kernel the most recent single-sequence decode used (TV_PATH_CTA or

@@ -39,14 +39,14 @@
 
 namespace tv {
 
-constexpr int GRID_THREADS = 640;    // largest block: the head's roles (N up to about 96)
+constexpr int GRID_THREADS = 640;    // largest block (96 registers a thread)
 constexpr int WORKER_THREADS = 256;  // a worker CTA keeps 8 warps; the rest exit at once
 constexpr int GRID_L = 8;            // head candidates d < L (a power of two)
 constexpr int CK_STRIDE = 32;      // checkpoint stride of the early window sums
 constexpr int PART_RING = 32;      // steps of worker partials in flight
 constexpr int SLOT_RING = 64;      // slot messages kept
 constexpr int SLOT_WORDS = 5;      // ctil (2), dsel (2), itil (1)
-constexpr int HEAD_GROUP = 4;      // lanes per state in the head (critical and helper warps)
+constexpr int HEAD_GROUP = 4;      // lanes per state in the head's matvec (2 when N is too large for 4)
 constexpr int GRID_MAX_N = 128;    // packed coarse scores keep the state index in 7 bits
 constexpr int COARSE_F = 14;       // fraction bits of the packed coarse matvec scores
 constexpr int COARSE_CLAMP = (1 << 23) - 1;
@@ -58,6 +58,8 @@ struct GridParams {
   long long chunk;  // largest worker range, in cells
   int max_seg;
   unsigned long long w_qd, w_dur, w_tr, w_ctil, w_dsel, w_acc0, w_acc1, w_itil, w_red, w_emw, w_bytes;
+  int w_global;                  // the window lives in global memory (L2), not in shared memory
+  unsigned long long w_gstride;  // bytes of one worker's window in global memory
   // head shared-memory offsets
   unsigned long long h_qcp, h_qtr, h_trh, h_dqcp, h_dq, h_ptil, h_base, h_dstar, h_ctil, h_itil, h_hwr, h_qd, h_dur,
       h_prek, h_pred, h_prei, h_prew, h_preq, h_pwq, h_pwk, h_pwd, h_pwi, h_psirec, h_tail, h_bytes;
@@ -66,6 +68,7 @@ struct GridParams {
   int st_threads;     // state helper threads: N rounded up to 32
   int in_threads;     // intake threads: S rounded up to 32
   int block;          // threads per CTA: the head's roles (at least WORKER_THREADS)
+  int head_group;     // matvec lanes per state in the head (4, or 2 for large N)
   int qf;             // fraction bits of the fixed-point scores
   int Np;             // N rounded up to 16 (packed coarse matvec rows)
   int cs_threads;     // critical-section threads (4 lanes per state, whole warps)
@@ -87,6 +90,7 @@ struct GridBufs {
   const double* ck;             // [D][M][N] checkpoints of the early window sums
   const double* hwin;           // [T][L][N] window sums E_t[d], d < L
   const long long* wrange;      // [G-1][2] worker cell ranges
+  unsigned char* wglob;         // [G-1][w_gstride] worker windows when they do not fit shared memory
   const int* seg_first;         // [N]
   const int* seg_count;         // [N]
   const int* seg_base;          // [G-1]
@@ -238,6 +242,11 @@ __device__ __forceinline__ void send_partial(const GridBufs& B, const GridParams
 // ---------------------------------------------------------------------------
 // Worker CTA (WORKER_THREADS threads)
 // ---------------------------------------------------------------------------
+// GW: the worker's window (slot scores, selected deltas, window sums, argmax
+// words) lives in a private global-memory buffer, served by L1/L2, and the
+// duration and transition rows are read from the model's tables; used when
+// N*D is too large for the workers' shared memory.
+template <bool GW>
 __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridBufs& B, unsigned char* sm) {
   constexpr int L = GRID_L;
   constexpr int NW = WORKER_THREADS / 32;
@@ -251,24 +260,30 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
   const int off0 = (int)(c_lo - (long long)ja * D);  // ring slot of the first cell
   const int seg0 = B.seg_base[w];
   const long long T = B.T;
-  long long* qd = (long long*)(sm + P.w_qd);          // [nseg][D]
-  double* dur = (double*)(sm + P.w_dur);              // [nseg][D]
-  double* tr = (double*)(sm + P.w_tr);                // [nseg][N]
-  long long* ctil = (long long*)(sm + P.w_ctil);      // [ncell]
-  double* dsel = (double*)(sm + P.w_dsel);            // [ncell]
-  double* acc_cur = (double*)(sm + P.w_acc0);         // [ncell] E_t
-  double* acc_nxt = (double*)(sm + P.w_acc1);         // [ncell] E_{t+1}
-  unsigned short* itil = (unsigned short*)(sm + P.w_itil);
+  unsigned char* wb = GW ? B.wglob + (size_t)w * P.w_gstride : sm;
+  long long* qd_s = (long long*)(sm + P.w_qd);        // [nseg][D]
+  double* dur_s = (double*)(sm + P.w_dur);            // [nseg][D]
+  double* tr_s = (double*)(sm + P.w_tr);              // [nseg][N]
+  const long long* qd = GW ? m.qdurT + (size_t)ja * D : qd_s;
+  const double* dur = GW ? m.durT + (size_t)ja * D : dur_s;
+  const double* tr = GW ? m.trans + (size_t)ja * N : tr_s;
+  long long* ctil = (long long*)(wb + P.w_ctil);      // [ncell]
+  double* dsel = (double*)(wb + P.w_dsel);            // [ncell]
+  double* acc_cur = (double*)(wb + P.w_acc0);         // [ncell] E_t
+  double* acc_nxt = (double*)(wb + P.w_acc1);         // [ncell] E_{t+1}
+  unsigned short* itil = (unsigned short*)(wb + P.w_itil);
   Top2* red = (Top2*)(sm + P.w_red);                  // [nseg][NW]
   ExactBest* ered = (ExactBest*)(sm + P.w_red);
   double* emw = (double*)(sm + P.w_emw);              // [2][max_seg] emission of the fold's step
   __shared__ int s_bad;
 
-  for (long long k = tid; k < (long long)nseg * D; k += WORKER_THREADS) {
-    qd[k] = m.qdurT[(size_t)ja * D + k];
-    dur[k] = m.durT[(size_t)ja * D + k];
+  if (!GW) {
+    for (long long k = tid; k < (long long)nseg * D; k += WORKER_THREADS) {
+      qd_s[k] = m.qdurT[(size_t)ja * D + k];
+      dur_s[k] = m.durT[(size_t)ja * D + k];
+    }
+    for (int k = tid; k < nseg * N; k += WORKER_THREADS) tr_s[k] = m.trans[(size_t)ja * N + k];
   }
-  for (int k = tid; k < nseg * N; k += WORKER_THREADS) tr[k] = m.trans[(size_t)ja * N + k];
   if (tid == 0) s_bad = 0;
   worker_sync();
 
@@ -551,9 +566,10 @@ __device__ __forceinline__ void packed_push(int p, int& b1, int& b2) {
   b2 = max(b2, lo);
 }
 
+template <int G4>
 __device__ __forceinline__ void group_reduce_exact(ExactBest& eb, unsigned gmask) {
 #pragma unroll
-  for (int o = HEAD_GROUP / 2; o > 0; o >>= 1) {
+  for (int o = G4 / 2; o > 0; o >>= 1) {
     const long long ok = __shfl_xor_sync(gmask, eb.k, o);
     const int od = __shfl_xor_sync(gmask, eb.d, o);
     const int oi = __shfl_xor_sync(gmask, eb.i, o);
@@ -574,12 +590,12 @@ __device__ __forceinline__ void take_partial(const TaggedMsg& pm, int k, int qf,
   pwi[k] = i;
 }
 
+template <int G4>
 __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBufs& B, unsigned char* sm) {
   constexpr int L = GRID_L;
-  constexpr int G4 = HEAD_GROUP;
   const int N = m.N, D = m.D, S = P.S, Np = P.Np;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const unsigned gmask = 0xfu << ((lane / G4) * G4);
+  const unsigned gmask = ((1u << G4) - 1) << ((lane / G4) * G4);
   const long long T = B.T;
   const long long margin = m.margin;
   int* Qcp = (int*)(sm + P.h_qcp);                    // [N][Np] packed coarse trans
@@ -1023,7 +1039,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
         const double* trj = trh + (size_t)j * N;
         for (int i = 0; i < N; ++i) eb.offer((e + row[i]) + trj[i], d, i);
       }
-      group_reduce_exact(eb, gmask);
+      group_reduce_exact<G4>(eb, gmask);
       if (gl == 0) {
         const int a = B.seg_first[j], b = a + B.seg_count[j];
         for (int k = a; k < b; ++k)
@@ -1062,13 +1078,14 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   }
 }
 
+template <bool GW, int G4>
 __global__ void __launch_bounds__(GRID_THREADS, 1) grid_decode_kernel(ModelView m, GridParams P, GridBufs B) {
   extern __shared__ __align__(16) unsigned char smem[];
   if (ld_relaxed_i32(B.abort_flag)) return;  // rejected observations
   if (blockIdx.x == 0) {
-    grid_head(m, P, B, smem);
+    grid_head<G4>(m, P, B, smem);
   } else if (threadIdx.x < WORKER_THREADS) {
-    grid_worker(m, P, B, smem);
+    grid_worker<GW>(m, P, B, smem);
   }
 }
 

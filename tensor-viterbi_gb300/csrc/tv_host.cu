@@ -121,8 +121,9 @@ struct tv_model_s {
   DevBuf<unsigned long long> msgs;  // slot messages, partial messages, exact delta ring
   DevBuf<double> dinit, ck, hwin;
   DevBuf<long long> wrange;
+  DevBuf<unsigned char> wglob;  // worker windows in global memory (large N*D)
   DevBuf<int> seg_first, seg_count, seg_base, gflags;
-  int plan_key_N = -1, plan_key_D = -1, plan_key_G = -1;
+  int plan_key_N = -1, plan_key_D = -1, plan_key_G = -1, plan_key_L2 = -1;
   tv::GridParams plan{};
   int path_pref = TV_PATH_AUTO, grid_ctas = 0, last_path = 0;
   // optional events around the main kernel
@@ -293,7 +294,7 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
 // its shared memory); otherwise the cells are cut into equal contiguous
 // chunks that may span several states.  A worker's intersection with a
 // state's row is a segment and yields one partial winner per step.
-bool plan_grid(tv_model_s* m, int G, int smem_optin, tv::GridParams& P, std::vector<long long>& wr,
+bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridParams& P, std::vector<long long>& wr,
                std::vector<int>& first, std::vector<int>& count, std::vector<int>& base) {
   const int N = m->N, D = m->D, L = tv::GRID_L;
   if (G < 2 || D <= L || N > tv::GRID_MAX_N || D > 65535) return false;
@@ -357,10 +358,34 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, tv::GridParams& P, std::vec
   P.w_red = o;  o = tv::tv_align(o + (unsigned long long)std::max(max_seg * (tv::WORKER_THREADS / 32) * sizeof(tv::Top2), 32 * sizeof(tv::ExactBest)));
   P.w_emw = o;  o = tv::tv_align(o + (unsigned long long)2 * max_seg * 8);
   P.w_bytes = o;
+  if (force_l2 || P.w_bytes + 256 > (unsigned long long)smem_optin) {
+    // The window does not fit the workers' shared memory: each worker keeps it
+    // in its own global-memory buffer (served by L1/L2) and reads the duration
+    // and transition rows from the model's tables.
+    P.w_global = 1;
+    unsigned long long g = 0;
+    P.w_ctil = g; g = tv::tv_align(g + (unsigned long long)chunk * 8);
+    P.w_dsel = g; g = tv::tv_align(g + (unsigned long long)chunk * 8);
+    P.w_acc0 = g; g = tv::tv_align(g + (unsigned long long)chunk * 8);
+    P.w_acc1 = g; g = tv::tv_align(g + (unsigned long long)chunk * 8);
+    P.w_itil = g; g = tv::tv_align(g + (unsigned long long)chunk * 2);
+    P.w_gstride = (g + 255) / 256 * 256;
+    o = 0;
+    P.w_qd = P.w_dur = P.w_tr = 0;
+    P.w_red = o;  o = tv::tv_align(o + (unsigned long long)std::max(max_seg * (tv::WORKER_THREADS / 32) * sizeof(tv::Top2), 32 * sizeof(tv::ExactBest)));
+    P.w_emw = o;  o = tv::tv_align(o + (unsigned long long)2 * max_seg * 8);
+    P.w_bytes = o;
+  }
   o = 0;
   const int Np = (N + 15) / 16 * 16;
   P.Np = Np;
-  P.cs_threads = (tv::HEAD_GROUP * N + 31) / 32 * 32;
+  // 4 matvec lanes per state when the roles fit the block, else 2
+  P.head_group = tv::HEAD_GROUP;
+  P.cs_threads = (P.head_group * N + 31) / 32 * 32;
+  if (P.cs_threads + (N + 31) / 32 * 32 + (S + 31) / 32 * 32 > tv::GRID_THREADS) {
+    P.head_group = 2;
+    P.cs_threads = (P.head_group * N + 31) / 32 * 32;
+  }
   P.cs_dense = (N + 31) / 32 * 32;
   P.st_threads = (N + 31) / 32 * 32;
   P.in_threads = (S + 31) / 32 * 32;
@@ -396,6 +421,14 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, tv::GridParams& P, std::vec
   P.h_bytes = o;
   P.timeout = 1LL << 31;  // SM clock cycles, about a second: no legitimate wait comes close
   return std::max(P.w_bytes, P.h_bytes) + 256 <= (unsigned long long)smem_optin;
+}
+
+// The grid kernel instance for a plan: window in shared or global memory,
+// 4 or 2 matvec lanes per state in the head.
+const void* grid_kernel_for(const tv::GridParams& P) {
+  if (P.w_global)
+    return P.head_group == 4 ? (const void*)tv::grid_decode_kernel<true, 4> : (const void*)tv::grid_decode_kernel<true, 2>;
+  return P.head_group == 4 ? (const void*)tv::grid_decode_kernel<false, 4> : (const void*)tv::grid_decode_kernel<false, 2>;
 }
 
 int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_dev, double* ll_dev,
@@ -448,6 +481,10 @@ int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_
   B.ck = m->ck.p;
   B.hwin = m->hwin.p;
   B.wrange = m->wrange.p;
+  if (P.w_global) {
+    if ((rc = m->wglob.ensure((size_t)(P.G - 1) * P.w_gstride)) != TV_OK) return rc;
+    B.wglob = m->wglob.p;
+  }
   B.seg_first = m->seg_first.p;
   B.seg_count = m->seg_count.p;
   B.seg_base = m->seg_base.p;
@@ -468,9 +505,10 @@ int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_
   }
   void* args[] = {&mv, &Pc, &B};
   const size_t dyn = std::max(P.w_bytes, P.h_bytes);
-  TV_CUDA(cudaFuncSetAttribute(tv::grid_decode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  const void* kern = grid_kernel_for(P);
+  TV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
   mark_start(m, st);
-  TV_CUDA(cudaLaunchCooperativeKernel((void*)tv::grid_decode_kernel, dim3(P.G), dim3(P.block), args, dyn, st));
+  TV_CUDA(cudaLaunchCooperativeKernel(kern, dim3(P.G), dim3(P.block), args, dyn, st));
   mark_end(m, st);
   m->last_launches += 1;
   return TV_OK;
@@ -489,23 +527,26 @@ int launch_single(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* pat
   const tv::CtaLayout L = tv::make_cta_layout(m->N, m->D);
   const bool cta_fits = L.bytes + 64 <= (size_t)smem_optin;
   int want = m->path_pref;
+  if (want == TV_PATH_GRID_L2) want = TV_PATH_GRID;
   if (want == TV_PATH_AUTO) want = cta_fits ? TV_PATH_CTA : TV_PATH_GRID;
   if (want == TV_PATH_GRID) {
     int per_sm = 0;
     int G = m->sm_count;
     if (m->grid_ctas > 0) G = std::min(G, m->grid_ctas);
-    if (m->plan_key_N != m->N || m->plan_key_D != m->D || m->plan_key_G != G) {
+    const int force_l2 = m->path_pref == TV_PATH_GRID_L2 ? 1 : 0;
+    if (m->plan_key_N != m->N || m->plan_key_D != m->D || m->plan_key_G != G || m->plan_key_L2 != force_l2) {
       std::vector<int> first, count, base;
       std::vector<long long> wr;
       tv::GridParams P;
-      if (!plan_grid(m, G, smem_optin, P, wr, first, count, base)) {
-        if (m->path_pref == TV_PATH_GRID)
-          return fail(TV_EINVAL, "the grid kernel cannot take this shape (needs D > 8, N <= 128, D <= 65535, and the per-CTA share of the window in shared memory)");
+      if (!plan_grid(m, G, smem_optin, force_l2 != 0, P, wr, first, count, base)) {
+        if (m->path_pref == TV_PATH_GRID || m->path_pref == TV_PATH_GRID_L2)
+          return fail(TV_EINVAL, "the grid kernel cannot take this shape (needs D > 8, D <= 65535, N small enough for the head CTA's tables and roles, about N <= 100)");
         want = TV_PATH_CTA;
       } else {
         const size_t dyn = std::max(P.w_bytes, P.h_bytes);
-        TV_CUDA(cudaFuncSetAttribute(tv::grid_decode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-        TV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tv::grid_decode_kernel, P.block, dyn));
+        const void* kern = grid_kernel_for(P);
+        TV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+        TV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, P.block, dyn));
         if (per_sm < 1) return fail(TV_EINVAL, "grid kernel does not fit on an SM");
         int rc;
         if ((rc = m->seg_first.ensure(first.size())) != TV_OK) return rc;
@@ -520,6 +561,7 @@ int launch_single(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* pat
         m->plan_key_N = m->N;
         m->plan_key_D = m->D;
         m->plan_key_G = G;
+        m->plan_key_L2 = force_l2;
       }
     }
     if (want == TV_PATH_GRID) {
@@ -679,7 +721,7 @@ int tv_model_destroy(tv_model m) {
 int64_t tv_model_last_launches(tv_model m) { return m ? m->last_launches : 0; }
 
 int tv_model_set_path(tv_model m, int path, int grid_ctas) {
-  if (!m || path < TV_PATH_AUTO || path > TV_PATH_GRID || grid_ctas < 0) return fail(TV_EINVAL, "bad path option");
+  if (!m || path < TV_PATH_AUTO || path > TV_PATH_GRID_L2 || grid_ctas < 0) return fail(TV_EINVAL, "bad path option");
   std::lock_guard<std::mutex> lk(m->mu);
   m->path_pref = path;
   m->grid_ctas = grid_ctas;

@@ -60,6 +60,7 @@ TV_STATIC_SCRATCH_BYTES = 32 << 20
 TV_PATH_AUTO = 0
 TV_PATH_CTA = 1
 TV_PATH_GRID = 2
+TV_PATH_GRID_L2 = 3
 
 
 def lib():

@@ -175,9 +175,12 @@ class Model:
 
     def set_path(self, path: str = "auto", grid_ctas: int = 0) -> None:
         """Kernel choice for single-sequence decodes: 'auto', 'cta' (one CTA,
-        window in its shared memory) or 'grid' (whole-GPU persistent grid);
-        grid_ctas > 0 caps the grid size.  Results are identical."""
-        code = {"auto": _lib.TV_PATH_AUTO, "cta": _lib.TV_PATH_CTA, "grid": _lib.TV_PATH_GRID}[path]
+        window in its shared memory), 'grid' (whole-GPU persistent grid) or
+        'grid-l2' (the grid with its window in global memory, as used when the
+        window does not fit the workers' shared memory); grid_ctas > 0 caps
+        the grid size.  Results are identical."""
+        code = {"auto": _lib.TV_PATH_AUTO, "cta": _lib.TV_PATH_CTA, "grid": _lib.TV_PATH_GRID,
+                "grid-l2": _lib.TV_PATH_GRID_L2}[path]
         _lib.check(_lib.lib().tv_model_set_path(self._h, code, int(grid_ctas)))
 
     def set_timing(self, enable: bool = True) -> None:

@@ -93,3 +93,69 @@ def test_grid_device_obs_validation(tvlib):
         path, ll = m.decode(p.obs_seq, return_loglik=True)
     np.testing.assert_array_equal(path, ref["path"])
     assert ll == ref["loglik"]
+
+
+@pytest.mark.parametrize("grid_ctas", [0, 7])
+@pytest.mark.parametrize("name", golden_names())
+def test_grid_window_in_l2_golden(tvlib, name, grid_ctas):
+    """The grid kernel with its window in global memory (the layout taken when
+    N*D does not fit the workers' shared memory), forced on every fixture."""
+    args, z = load_golden(name)
+    N, D = args[0], args[5].shape[0]
+    if not _grid_ok(N, D):
+        pytest.skip("shape outside the grid kernel (D <= 8)")
+    ref = orc.decode(*args)
+    with tvlib.Model(*args[:6]) as m:
+        m.set_path("grid-l2", grid_ctas)
+        path, ll = m.decode(args[6], return_loglik=True)
+        assert m.last_path() == "grid"
+    np.testing.assert_array_equal(path, z["path_cpp"])
+    assert ll == ref["loglik"]
+
+
+def test_grid_large_n_two_lane_head(tvlib):
+    """N = 100: the head's matvec runs two lanes per state (four do not fit the
+    block beside the other roles); both window placements."""
+    import tensor_viterbi.synthetic as syn
+    p = syn.discrete_problem(100, 40, 700, 24, 5.0, 30.0, seed=11)
+    ref = orc.decode(*p.args(), variant="omp")
+    with tvlib.Model(*p.model_args()) as m:
+        for kind in ("grid", "grid-l2"):
+            m.set_path(kind, 0)
+            path, ll = m.decode(p.obs_seq, return_loglik=True)
+            assert m.last_path() == "grid"
+            np.testing.assert_array_equal(path, ref["path"])
+            assert ll == ref["loglik"]
+
+
+def _segments_of(path, D):
+    starts = np.flatnonzero(np.diff(path, prepend=-1) != 0)
+    lengths = np.diff(np.append(starts, path.size))
+    seg = np.zeros(path.size, dtype=np.uint8)
+    seg[starts] = 1
+    return seg, lengths
+
+
+def test_stress_shape_window_in_l2_properties(tvlib):
+    """The stress shape's window (N = 100, D = 1e4: 1e6 cells, too large for
+    shared memory, so the grid picks the global-memory window) on a 3e4-step
+    sequence.  The oracle's O(T N^2 D) recursion is out of reach at this
+    size, so size-independent properties stand in: every segment fits the
+    duration range, the returned log-likelihood is the long-double score of
+    the returned path within 1e-9 relative, and a second decode is identical.
+    Exactness itself is covered by the parity tests of the same kernel on
+    smaller shapes above."""
+    import tensor_viterbi.synthetic as syn
+    p = syn.discrete_problem(100, 10_000, 30_000, 64, 5.0, 50.0, seed=4)
+    with tvlib.Model(*p.model_args()) as m:
+        path, ll = m.decode(p.obs_seq, return_loglik=True)
+        assert m.last_path() == "grid"
+        path2, ll2 = m.decode(p.obs_seq, return_loglik=True)
+    np.testing.assert_array_equal(path, path2)
+    assert ll == ll2
+    assert path.min() >= 0 and path.max() < 100
+    seg, lengths = _segments_of(path, 10_000)
+    assert lengths.max() <= 10_000
+    sc = orc.score_segments(p.n_states, p.trans_mat, p.emission_probs, p.start_probs, p.duration_probs,
+                            p.obs_seq, path, seg)
+    assert abs(ll - sc) <= 1e-9 * abs(sc)
