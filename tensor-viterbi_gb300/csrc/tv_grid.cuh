@@ -40,7 +40,8 @@
 namespace tv {
 
 constexpr int GRID_THREADS = 640;    // largest block (96 registers a thread)
-constexpr int WORKER_THREADS = 256;  // a worker CTA keeps 8 warps; the rest exit at once
+constexpr int WORKER_THREADS = 256;     // a worker CTA keeps 8 warps (window in shared memory); the rest exit
+constexpr int WORKER_THREADS_GW = 512;  // 16 warps when the window is in global memory (more loads in flight)
 constexpr int GRID_L = 8;            // head candidates d < L (a power of two)
 constexpr int CK_STRIDE = 32;      // checkpoint stride of the early window sums
 constexpr int PART_RING = 32;      // steps of worker partials in flight
@@ -64,6 +65,7 @@ struct GridParams {
   unsigned long long h_qcp, h_qtr, h_trh, h_dqcp, h_dq, h_ptil, h_base, h_dstar, h_ctil, h_itil, h_hwr, h_qd, h_dur,
       h_prek, h_pred, h_prei, h_prew, h_preq, h_pwq, h_pwk, h_pwd, h_pwi, h_psirec, h_tail, h_bytes;
   int trans_smem;     // the exact transition matrix is kept in the head's shared memory
+  int qtr_smem;       // so is its fixed-point copy (else computed from the exact one)
   int cs_dense;       // critical threads of the dense (one lane per state) phase: N rounded up to 32
   int st_threads;     // state helper threads: N rounded up to 32
   int in_threads;     // intake threads: S rounded up to 32
@@ -212,21 +214,23 @@ __device__ __forceinline__ bool load_dstar(const GridBufs& B, const GridParams& 
 // The non-aligned barrier counts threads, so lanes of a warp may arrive apart
 // (after a lane-0 wait, say); the aligned bar.sync would need the warp
 // converged, which the compiler does not ensure before inline assembly.
+template <int WT>
 __device__ __forceinline__ void worker_sync() {
-  asm volatile("barrier.sync 1, %0;" ::"r"(WORKER_THREADS) : "memory");
+  asm volatile("barrier.sync 1, %0;" ::"r"(WT) : "memory");
 }
 
 // Block-wide reduction of an ExactBest over the worker threads; every worker
 // thread receives the result.
+template <int WT>
 __device__ __forceinline__ ExactBest worker_reduce_exact(ExactBest eb, ExactBest* scratch) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   eb.warp_reduce();
-  worker_sync();
+  worker_sync<WT>();
   if (lane == 0) scratch[warp] = eb;
-  worker_sync();
+  worker_sync<WT>();
   ExactBest r;
   r.init();
-  if (lane < WORKER_THREADS / 32) r = scratch[lane];
+  if (lane < WT / 32) r = scratch[lane];
   r.warp_reduce();
   return r;
 }
@@ -240,7 +244,7 @@ __device__ __forceinline__ void send_partial(const GridBufs& B, const GridParams
 }
 
 // ---------------------------------------------------------------------------
-// Worker CTA (WORKER_THREADS threads)
+// Worker CTA (WORKER_THREADS threads, WORKER_THREADS_GW with the window in global memory)
 // ---------------------------------------------------------------------------
 // GW: the worker's window (slot scores, selected deltas, window sums, argmax
 // words) lives in a private global-memory buffer, served by L1/L2, and the
@@ -249,7 +253,8 @@ __device__ __forceinline__ void send_partial(const GridBufs& B, const GridParams
 template <bool GW>
 __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridBufs& B, unsigned char* sm) {
   constexpr int L = GRID_L;
-  constexpr int NW = WORKER_THREADS / 32;
+  constexpr int WT = GW ? WORKER_THREADS_GW : WORKER_THREADS;
+  constexpr int NW = WT / 32;
   const int N = m.N, D = m.D;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int w = blockIdx.x - 1;
@@ -278,14 +283,14 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
   __shared__ int s_bad;
 
   if (!GW) {
-    for (long long k = tid; k < (long long)nseg * D; k += WORKER_THREADS) {
+    for (long long k = tid; k < (long long)nseg * D; k += WT) {
       qd_s[k] = m.qdurT[(size_t)ja * D + k];
       dur_s[k] = m.durT[(size_t)ja * D + k];
     }
-    for (int k = tid; k < nseg * N; k += WORKER_THREADS) tr_s[k] = m.trans[(size_t)ja * N + k];
+    for (int k = tid; k < nseg * N; k += WT) tr_s[k] = m.trans[(size_t)ja * N + k];
   }
   if (tid == 0) s_bad = 0;
-  worker_sync();
+  worker_sync<WT>();
 
   auto seg_of = [&](int s, int& rb, int& re) {
     rb = (s == 0) ? off0 : 0;
@@ -303,7 +308,7 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
     if (3 < T) em_pf = m.em[(size_t)B.obs[3] * N + j];
     if (4 < T) ob_pf = B.obs[4];
   }
-  worker_sync();
+  worker_sync<WT>();
 
   int r0 = 0;  // (t-1) % D
   for (long long t = 1; t < T; ++t) {
@@ -333,7 +338,8 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
       const double em1 = fold ? emw[(int)(t1 & 1) * P.max_seg + s] : 0.0;
       Top2 tb;
       tb.init();
-      for (int r = rb + tid; r < re; r += WORKER_THREADS) {
+#pragma unroll 4
+      for (int r = rb + tid; r < re; r += WT) {
         int d = r0 - r;
         if (d < 0) d += D;
         if (d >= L && d < tau) tb.push(ct[r] + q[d], d);
@@ -342,7 +348,7 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
       tb.warp_reduce();
       if (lane == 0) red[s * NW + warp] = tb;
     }
-    worker_sync();
+    worker_sync<WT>();
 
     // Phase 2a: certified exact winner per segment (warps take segments in
     // turn), sent to the head.
@@ -449,7 +455,7 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
         const int j = ja + s;
         const double em1 = m.em[(size_t)ot1 * N + j];
         double* an = acc_nxt + s * D - off0;
-        for (int r = rb + tid; r < re; r += WORKER_THREADS) {
+        for (int r = rb + tid; r < re; r += WT) {
           int d = r0n - r;
           if (d < 0) d += D;
           const double base = (d == 0) ? 0.0 : early_window(m, B.ck, P.M, B.obs, D, d - 1, j);
@@ -457,7 +463,7 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
         }
       }
     }
-    worker_sync();
+    worker_sync<WT>();
     if (s_bad) return;
     if (fold || seed) {
       double* x = acc_cur;
@@ -480,7 +486,7 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
       ExactBest eb;
       eb.init();
       bool ok = true;
-      for (int r = rb + tid; r < re && ok; r += WORKER_THREADS) {
+      for (int r = rb + tid; r < re && ok; r += WT) {
         int d = rt - r;
         if (d < 0) d += D;
         if (d < L || d >= tau) continue;
@@ -497,7 +503,7 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
         grid_fail(B, TV_ETIMEOUT_DEV, SITE_WORKER_TAIL);
         s_bad = 1;
       }
-      eb = worker_reduce_exact(eb, ered);
+      eb = worker_reduce_exact<WT>(eb, ered);
       if (s_bad) return;
       if (tid == 0) send_partial(B, P, (unsigned)T, (unsigned)T & (PART_RING - 1), seg0 + s, eb);
     }
@@ -599,9 +605,16 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   const long long T = B.T;
   const long long margin = m.margin;
   int* Qcp = (int*)(sm + P.h_qcp);                    // [N][Np] packed coarse trans
-  long long* qtr = (long long*)(sm + P.h_qtr);        // [N][N] fine trans
+  long long* qtr_s = (long long*)(sm + P.h_qtr);      // [N][N] fine trans (when it fits)
   double* trh_s = (double*)(sm + P.h_trh);            // [N][N] exact trans (when it fits)
   const double* trh = P.trans_smem ? trh_s : m.trans;
+  // fixed-point transition score: the shared copy, else quantised from the
+  // exact table (the same rounding as the copy), else the global copy
+  auto qtr_at = [&](int j, int i) -> long long {
+    if (P.qtr_smem) return qtr_s[j * N + i];
+    if (P.trans_smem) return quantize(trh_s[j * N + i], m.scale);
+    return m.qtr[(size_t)j * N + i];
+  };
   int* dqcp = (int*)(sm + P.h_dqcp);                  // [2][Np] packed coarse delta
   long long* dq = (long long*)(sm + P.h_dq);          // [2][N] fine delta
   long long* ptil = (long long*)(sm + P.h_ptil);      // [4][N] emission prefix P(t), row t % 4
@@ -660,7 +673,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
     }
   }
   for (int k = tid; k < N * N; k += blockDim.x) {
-    qtr[k] = m.qtr[k];
+    if (P.qtr_smem) qtr_s[k] = m.qtr[k];
     if (P.trans_smem) trh_s[k] = m.trans[k];
   }
   for (int k = tid; k < N * L; k += blockDim.x) {
@@ -778,12 +791,15 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
         bool amb = ((b1 >> 7) - (b2 >> 7)) <= P.coarse_margin;
         long long bfine;
         if (!amb) {
-          bfine = qtr[j * N + ifine] + dq[prv * N + ifine];
+          bfine = qtr_at(j, ifine) + dq[prv * N + ifine];
         } else {
           // fine int64 pass decides (and certifies with the fine margin)
           Top2 tb;
           tb.init();
-          for (int i = gl; i < N; i += G4) tb.push(qtr[j * N + i] + dq[prv * N + i], i);
+          // (a whole row: the shared copy, else the global one, whose loads
+          // are independent and overlap, unlike N dependent conversions)
+          const long long* qrow_f = P.qtr_smem ? qtr_s + (size_t)j * N : m.qtr + (size_t)j * N;
+          for (int i = gl; i < N; i += G4) tb.push(qrow_f[i] + dq[prv * N + i], i);
 #pragma unroll
           for (int o = G4 / 2; o > 0; o >>= 1) {
             const long long ob1 = __shfl_xor_sync(gmask, tb.b1, o);
@@ -1084,7 +1100,7 @@ __global__ void __launch_bounds__(GRID_THREADS, 1) grid_decode_kernel(ModelView 
   if (ld_relaxed_i32(B.abort_flag)) return;  // rejected observations
   if (blockIdx.x == 0) {
     grid_head<G4>(m, P, B, smem);
-  } else if (threadIdx.x < WORKER_THREADS) {
+  } else if (threadIdx.x < (GW ? WORKER_THREADS_GW : WORKER_THREADS)) {
     grid_worker<GW>(m, P, B, smem);
   }
 }

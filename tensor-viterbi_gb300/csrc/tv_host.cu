@@ -300,68 +300,110 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
   if (G < 2 || D <= L || N > tv::GRID_MAX_N || D > 65535) return false;
   const int Gw = G - 1;
   const long long ND = (long long)N * D;
-  wr.assign(2 * (size_t)Gw, 0);
   long long chunk = 0;
-  const int k = Gw / N;
-  if (k >= 1) {
-    const int parts = (int)std::min<long long>(k, D);
-    const long long part = (D + parts - 1) / parts;
-    int w = 0;
-    for (int j = 0; j < N; ++j)
-      for (int q = 0; q < parts; ++q, ++w) {
-        const long long lo = (long long)j * D + (long long)q * part;
-        const long long hi = std::min((long long)j * D + (long long)(q + 1) * part, (long long)(j + 1) * D);
-        wr[2 * w] = lo;
-        wr[2 * w + 1] = std::max(lo, hi);
-      }
-    for (; w < Gw; ++w) wr[2 * w] = wr[2 * w + 1] = ND;
-    chunk = part;
-  } else {
-    chunk = (ND + Gw - 1) / Gw;
-    for (int w = 0; w < Gw; ++w) {
-      const long long lo = std::min((long long)w * chunk, ND), hi = std::min(lo + chunk, ND);
-      wr[2 * w] = lo;
-      wr[2 * w + 1] = hi;
-    }
-  }
-  first.assign(N, 0);
-  count.assign(N, 0);
-  base.assign(Gw, 0);
-  std::vector<int> seen(N, 0);
   int S = 0, max_seg = 0;
-  for (int w = 0; w < Gw; ++w) {
-    const long long lo = wr[2 * w], hi = wr[2 * w + 1];
-    base[w] = S;
-    if (lo >= hi) continue;
-    const int ja = (int)(lo / D), jb = (int)((hi - 1) / D);
-    for (int j = ja; j <= jb; ++j) {
-      if (!seen[j]) { seen[j] = 1; first[j] = S; }
-      count[j]++;
-      S++;
+  auto partition = [&](bool row_aligned) {
+    wr.assign(2 * (size_t)Gw, 0);
+    const int k = Gw / N;
+    if (row_aligned && k >= 1) {
+      const int parts = (int)std::min<long long>(k, D);
+      const long long part = (D + parts - 1) / parts;
+      int w = 0;
+      for (int j = 0; j < N; ++j)
+        for (int q = 0; q < parts; ++q, ++w) {
+          const long long lo = (long long)j * D + (long long)q * part;
+          const long long hi = std::min((long long)j * D + (long long)(q + 1) * part, (long long)(j + 1) * D);
+          wr[2 * w] = lo;
+          wr[2 * w + 1] = std::max(lo, hi);
+        }
+      for (; w < Gw; ++w) wr[2 * w] = wr[2 * w + 1] = ND;
+      chunk = part;
+    } else {
+      chunk = (ND + Gw - 1) / Gw;
+      for (int w = 0; w < Gw; ++w) {
+        const long long lo = std::min((long long)w * chunk, ND), hi = std::min(lo + chunk, ND);
+        wr[2 * w] = lo;
+        wr[2 * w + 1] = hi;
+      }
     }
-    max_seg = std::max(max_seg, jb - ja + 1);
+    first.assign(N, 0);
+    count.assign(N, 0);
+    base.assign(Gw, 0);
+    std::vector<int> seen(N, 0);
+    S = 0;
+    max_seg = 0;
+    for (int w = 0; w < Gw; ++w) {
+      const long long lo = wr[2 * w], hi = wr[2 * w + 1];
+      base[w] = S;
+      if (lo >= hi) continue;
+      const int ja = (int)(lo / D), jb = (int)((hi - 1) / D);
+      for (int j = ja; j <= jb; ++j) {
+        if (!seen[j]) { seen[j] = 1; first[j] = S; }
+        count[j]++;
+        S++;
+      }
+      max_seg = std::max(max_seg, jb - ja + 1);
+    }
+  };
+  // Head roles: 4 matvec lanes per state when everything fits the block, else 2.
+  auto head_roles_fit = [&](int S_) {
+    const int st = (N + 31) / 32 * 32, in = (S_ + 31) / 32 * 32;
+    return (2 * N + 31) / 32 * 32 + st + in <= tv::GRID_THREADS;
+  };
+  // Cells are split per state (row-aligned) when every state gets whole
+  // workers, so that a worker's duration and transition rows are one state's;
+  // otherwise in equal contiguous chunks that may span states.
+  partition(true);
+  // Window in shared memory when a worker's share fits there: the duration
+  // rows (8 B fixed point + 8 B exact per d) and transition rows of its
+  // states, and per cell the slot score, selected delta, two window-sum
+  // buffers (8 B each) and the argmax word (2 B).
+  auto smem_window_bytes = [&]() {
+    unsigned long long o = 0;
+    o = tv::tv_align(o + (unsigned long long)max_seg * D * 8);
+    o = tv::tv_align(o + (unsigned long long)max_seg * D * 8);
+    o = tv::tv_align(o + (unsigned long long)max_seg * N * 8);
+    for (int a = 0; a < 4; ++a) o = tv::tv_align(o + (unsigned long long)chunk * 8);
+    o = tv::tv_align(o + (unsigned long long)chunk * 2);
+    o = tv::tv_align(o + (unsigned long long)std::max(max_seg * (tv::WORKER_THREADS / 32) * sizeof(tv::Top2), 32 * sizeof(tv::ExactBest)));
+    o = tv::tv_align(o + (unsigned long long)2 * max_seg * 8);
+    return o;
+  };
+  const bool global_window = force_l2 || smem_window_bytes() + 256 > (unsigned long long)smem_optin;
+  if (global_window) {
+    // In global memory the tables come from the model, so equal contiguous
+    // chunks over all workers balance the scan best, as long as the head's
+    // intake roles (one lane per segment) still fit.
+    std::vector<long long> wr0 = wr;
+    std::vector<int> f0 = first, c0 = count, b0 = base;
+    const long long chunk0 = chunk;
+    const int S0 = S, ms0 = max_seg;
+    partition(false);
+    if (!head_roles_fit(S) || max_seg > 32) {
+      wr = wr0; first = f0; count = c0; base = b0; chunk = chunk0; S = S0; max_seg = ms0;
+    }
   }
-  if (S > tv::GRID_THREADS || max_seg > 32) return false;
+  if (S > tv::GRID_THREADS || max_seg > 32 || !head_roles_fit(S)) return false;
   P = tv::GridParams{};
   P.G = G; P.L = L; P.S = S; P.Rd = D + 2 * L + 8;
   P.M = (D + tv::CK_STRIDE - 1) / tv::CK_STRIDE;
   P.chunk = chunk; P.max_seg = max_seg;
   unsigned long long o = 0;
-  P.w_qd = o;   o = tv::tv_align(o + (unsigned long long)max_seg * D * 8);
-  P.w_dur = o;  o = tv::tv_align(o + (unsigned long long)max_seg * D * 8);
-  P.w_tr = o;   o = tv::tv_align(o + (unsigned long long)max_seg * N * 8);
-  P.w_ctil = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
-  P.w_dsel = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
-  P.w_acc0 = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
-  P.w_acc1 = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
-  P.w_itil = o; o = tv::tv_align(o + (unsigned long long)chunk * 2);
-  P.w_red = o;  o = tv::tv_align(o + (unsigned long long)std::max(max_seg * (tv::WORKER_THREADS / 32) * sizeof(tv::Top2), 32 * sizeof(tv::ExactBest)));
-  P.w_emw = o;  o = tv::tv_align(o + (unsigned long long)2 * max_seg * 8);
-  P.w_bytes = o;
-  if (force_l2 || P.w_bytes + 256 > (unsigned long long)smem_optin) {
-    // The window does not fit the workers' shared memory: each worker keeps it
-    // in its own global-memory buffer (served by L1/L2) and reads the duration
-    // and transition rows from the model's tables.
+  if (!global_window) {
+    P.w_qd = o;   o = tv::tv_align(o + (unsigned long long)max_seg * D * 8);
+    P.w_dur = o;  o = tv::tv_align(o + (unsigned long long)max_seg * D * 8);
+    P.w_tr = o;   o = tv::tv_align(o + (unsigned long long)max_seg * N * 8);
+    P.w_ctil = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
+    P.w_dsel = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
+    P.w_acc0 = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
+    P.w_acc1 = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
+    P.w_itil = o; o = tv::tv_align(o + (unsigned long long)chunk * 2);
+    P.w_red = o;  o = tv::tv_align(o + (unsigned long long)std::max(max_seg * (tv::WORKER_THREADS / 32) * sizeof(tv::Top2), 32 * sizeof(tv::ExactBest)));
+    P.w_emw = o;  o = tv::tv_align(o + (unsigned long long)2 * max_seg * 8);
+    P.w_bytes = o;
+  } else {
+    // Each worker keeps its window in its own global-memory buffer (served by
+    // L1/L2) and reads the duration and transition rows from the model.
     P.w_global = 1;
     unsigned long long g = 0;
     P.w_ctil = g; g = tv::tv_align(g + (unsigned long long)chunk * 8);
@@ -370,9 +412,8 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
     P.w_acc1 = g; g = tv::tv_align(g + (unsigned long long)chunk * 8);
     P.w_itil = g; g = tv::tv_align(g + (unsigned long long)chunk * 2);
     P.w_gstride = (g + 255) / 256 * 256;
-    o = 0;
     P.w_qd = P.w_dur = P.w_tr = 0;
-    P.w_red = o;  o = tv::tv_align(o + (unsigned long long)std::max(max_seg * (tv::WORKER_THREADS / 32) * sizeof(tv::Top2), 32 * sizeof(tv::ExactBest)));
+    P.w_red = o;  o = tv::tv_align(o + (unsigned long long)std::max(max_seg * (tv::WORKER_THREADS_GW / 32) * sizeof(tv::Top2), 32 * sizeof(tv::ExactBest)));
     P.w_emw = o;  o = tv::tv_align(o + (unsigned long long)2 * max_seg * 8);
     P.w_bytes = o;
   }
@@ -389,10 +430,9 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
   P.cs_dense = (N + 31) / 32 * 32;
   P.st_threads = (N + 31) / 32 * 32;
   P.in_threads = (S + 31) / 32 * 32;
-  P.block = std::max(P.cs_threads + P.st_threads + P.in_threads, tv::WORKER_THREADS);
+  P.block = std::max(P.cs_threads + P.st_threads + P.in_threads, P.w_global ? tv::WORKER_THREADS_GW : tv::WORKER_THREADS);
   if (P.block > tv::GRID_THREADS) return false;
   P.h_qcp = o;    o = tv::tv_align(o + (unsigned long long)N * Np * 4);
-  P.h_qtr = o;    o = tv::tv_align(o + (unsigned long long)N * N * 8);
   P.h_dqcp = o;   o = tv::tv_align(o + (unsigned long long)2 * Np * 4);
   P.h_dq = o;     o = tv::tv_align(o + (unsigned long long)2 * N * 8);
   P.h_ptil = o;   o = tv::tv_align(o + (unsigned long long)4 * N * 8);
@@ -414,10 +454,16 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
   P.h_pwi = o;    o = tv::tv_align(o + (unsigned long long)S * 4);
   P.h_psirec = o; o = tv::tv_align(o + (unsigned long long)2 * N * 4);
   P.h_tail = o;   o = tv::tv_align(o + (unsigned long long)N * 8);
-  // the exact transition matrix joins the head's shared memory when it fits
+  // The exact transition matrix and its fixed-point copy join the head's
+  // shared memory when they fit; the exact one first (the fixed-point copy
+  // is then computed from it: a multiply and a conversion).
+  const unsigned long long nn8 = tv::tv_align((unsigned long long)N * N * 8);
   P.h_trh = o;
-  P.trans_smem = o + (unsigned long long)N * N * 8 + 256 <= (unsigned long long)smem_optin ? 1 : 0;
-  if (P.trans_smem) o = tv::tv_align(o + (unsigned long long)N * N * 8);
+  P.trans_smem = o + nn8 + 256 <= (unsigned long long)smem_optin ? 1 : 0;
+  if (P.trans_smem) o += nn8;
+  P.h_qtr = o;
+  P.qtr_smem = o + nn8 + 256 <= (unsigned long long)smem_optin ? 1 : 0;
+  if (P.qtr_smem) o += nn8;
   P.h_bytes = o;
   P.timeout = 1LL << 31;  // SM clock cycles, about a second: no legitimate wait comes close
   return std::max(P.w_bytes, P.h_bytes) + 256 <= (unsigned long long)smem_optin;
