@@ -153,6 +153,60 @@ int tv_decode_device_static(tv_model m, const int32_t* obs_dev, int64_t T,
                             int32_t* path_dev, double* loglik_dev, int* status_dev,
                             void* stream);
 
+/* ---- Gaussian emissions (no reference counterpart: the reference takes a
+ * discrete emission table only; a per-timestep table with obs = 0..T-1 is
+ * the same decode) ----
+ *
+ * tv_gaussian_loglik: the emission front-end on the device.  table_dev
+ * (T x N, row t = observation t) receives log N(x_t; mean_j, sd_j) =
+ * ((-0.5 z) z - log sd_j) - log(2 pi)/2 with z = (x_t - mean_j) / sd_j, every
+ * operation rounded once in FP64 and log sd_j, log(2 pi) taken on the host
+ * with the C library's log, so the table equals that expression evaluated on
+ * the host.  x_dev is a device array of T doubles; mean and sd are host
+ * arrays of N.  Asynchronous on `stream`.
+ *
+ * tv_model_create_gaussian: a model whose emission table is built that way
+ * from host observations x (T doubles); decode it with obs = 0..T-1. */
+int tv_gaussian_loglik(const double* x_dev, int64_t T, int n_states, const double* mean,
+                       const double* sd, double* table_dev, void* stream);
+int tv_model_create_gaussian(int n_states, int max_dur, int64_t T, const double* trans_mat,
+                             const double* duration_probs_linear, const double* start_probs,
+                             const double* duration_probs, const double* x, const double* mean,
+                             const double* sd, tv_model* out);
+
+/* ---- Decode server (no reference counterpart): continuous batching of
+ * independent requests, each with its own model. ----
+ *
+ * A scheduler thread admits submitted requests in arrival order while the
+ * device-memory budget allows (budget_bytes <= 0: 80% of the free memory)
+ * and one of max_inflight streams is free (<= 0: 64).  Each admitted request
+ * runs on its own stream with its own model and buffers, allocated in stream
+ * order, so requests overlap on the GPU and each result is the one a decode
+ * alone gives.  Submission copies the inputs and returns a ticket >= 0 (or a
+ * negative status).  tv_server_poll returns 1 and writes the path (T int32),
+ * the log-likelihood and latency_ms_out[0..1] = {submission to completion,
+ * submission to admission} when the request is done (the ticket is then
+ * released), 0 while it is pending, or the request's negative status;
+ * tv_server_wait blocks until done.  tv_server_stats writes 8 counters:
+ * admitted, completed, failed, running, pending, bytes in use, peak bytes in
+ * use, budget.  tv_server_destroy finishes the requests in flight. */
+typedef struct tv_server_s* tv_server;
+tv_server tv_server_create(int64_t budget_bytes, int max_inflight);
+int tv_server_destroy(tv_server s);
+int64_t tv_server_submit(tv_server s, int n_states, int n_symbols, int max_dur, int64_t T,
+                         const double* trans_mat, const double* emission_probs,
+                         const double* duration_probs_linear, const double* start_probs,
+                         const double* duration_probs, const int32_t* obs_seq);
+int64_t tv_server_submit_gaussian(tv_server s, int n_states, int max_dur, int64_t T,
+                                  const double* trans_mat, const double* duration_probs_linear,
+                                  const double* start_probs, const double* duration_probs,
+                                  const double* x, const double* mean, const double* sd);
+int tv_server_poll(tv_server s, int64_t ticket, int32_t* path_out, double* loglik_out,
+                   double* latency_ms_out);
+int tv_server_wait(tv_server s, int64_t ticket, int32_t* path_out, double* loglik_out,
+                   double* latency_ms_out);
+int tv_server_stats(tv_server s, int64_t* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,30 +39,56 @@ int fail(int code, const std::string& msg) {
       return fail(TV_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
   } while (0)
 
+// Stream-ordered allocation for the calling thread: while set (the decode
+// server's scheduler sets it around each request), device buffers come from
+// the device's memory pool in the order of that stream and are freed the same
+// way, so finishing one request never waits for the others (cudaFree would
+// synchronise the whole device).  Uploads into such buffers go on the same
+// stream.
+thread_local cudaStream_t g_alloc_stream = nullptr;
+thread_local bool g_alloc_async = false;
+
 template <class T>
 struct DevBuf {
   T* p = nullptr;
   size_t n = 0;
+  cudaStream_t st = nullptr;  // stream-ordered buffer: its stream
+  bool async = false;
   int ensure(size_t count) {
     if (count <= n && p) return TV_OK;
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
+    release();
     if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    cudaError_t e;
+    if (g_alloc_async) {
+      e = cudaMallocAsync((void**)&p, count * sizeof(T), g_alloc_stream);
+      st = g_alloc_stream;
+      async = true;
+    } else {
+      e = cudaMalloc(&p, count * sizeof(T));
+      async = false;
+    }
     if (e != cudaSuccess) {
       p = nullptr;
-      return fail(TV_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+      return fail(TV_ENOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
     }
     n = count;
     return TV_OK;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (async) cudaFreeAsync(p, st);
+      else cudaFree(p);
+    }
     p = nullptr;
     n = 0;
   }
 };
+
+// Host-to-device upload on the thread's allocation stream when set.
+cudaError_t upload(void* dst, const void* src, size_t bytes) {
+  if (g_alloc_async) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, g_alloc_stream);
+  return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+}
 
 constexpr int kThreads = 256;
 
@@ -599,10 +625,10 @@ int launch_single(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* pat
         if ((rc = m->seg_count.ensure(count.size())) != TV_OK) return rc;
         if ((rc = m->seg_base.ensure(base.size())) != TV_OK) return rc;
         if ((rc = m->wrange.ensure(wr.size())) != TV_OK) return rc;
-        TV_CUDA(cudaMemcpy(m->wrange.p, wr.data(), sizeof(long long) * wr.size(), cudaMemcpyHostToDevice));
-        TV_CUDA(cudaMemcpy(m->seg_first.p, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice));
-        TV_CUDA(cudaMemcpy(m->seg_count.p, count.data(), sizeof(int) * count.size(), cudaMemcpyHostToDevice));
-        TV_CUDA(cudaMemcpy(m->seg_base.p, base.data(), sizeof(int) * base.size(), cudaMemcpyHostToDevice));
+        TV_CUDA(upload(m->wrange.p, wr.data(), sizeof(long long) * wr.size()));
+        TV_CUDA(upload(m->seg_first.p, first.data(), sizeof(int) * first.size()));
+        TV_CUDA(upload(m->seg_count.p, count.data(), sizeof(int) * count.size()));
+        TV_CUDA(upload(m->seg_base.p, base.data(), sizeof(int) * base.size()));
         m->plan = P;
         m->plan_key_N = m->N;
         m->plan_key_D = m->D;
@@ -696,24 +722,67 @@ int static_scratch_for_current_device(unsigned char** out) {
   return TV_OK;
 }
 
-}  // namespace
 
-extern "C" {
+// Finite check and max |x| of a device table (the emission table built on the
+// device by the Gaussian front-end): out[0] = bits of max |x| (non-negative
+// doubles order as their bit patterns), out[1] = 1 if any entry is not finite.
+__global__ void absmax_kernel(const double* __restrict__ a, size_t n, unsigned long long* out) {
+  unsigned long long mx = 0;
+  unsigned long long bad = 0;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const double v = a[k];
+    if (!isfinite(v)) bad = 1;
+    else mx = max(mx, (unsigned long long)__double_as_longlong(fabs(v)));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(out, mx);
+    if (bad) atomicOr(out + 1, 1ull);
+  }
+}
 
-const char* tv_last_error(void) { return g_err.c_str(); }
+// Gaussian emission front-end: table[t][j] = log N(x_t; mu_j, sd_j)
+// = ((-0.5 * z) * z - log sd_j) - log(2 pi)/2 with z = (x_t - mu_j) / sd_j,
+// each operation rounded once (no fused multiply-add), so the table equals
+// the same expression evaluated in FP64 on the host given the same log sd_j
+// and constant (computed on the host with the C library's log).
+__global__ void gaussian_loglik_kernel(const double* __restrict__ x, long long T, int N, const double* __restrict__ mu,
+                                       const double* __restrict__ sd, const double* __restrict__ logsd, double c,
+                                       double* __restrict__ table) {
+  const long long n = T * N;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const long long t = k / N;
+    const int j = (int)(k - t * N);
+    const double z = __ddiv_rn(__dsub_rn(x[t], mu[j]), sd[j]);
+    table[k] = __dsub_rn(__dsub_rn(__dmul_rn(__dmul_rn(-0.5, z), z), logsd[j]), c);
+  }
+}
 
-int tv_model_create(int N, int O, int D, const double* trans, const double* emission,
-                    const double* dur_lin, const double* start, const double* dur, tv_model* out) {
-  (void)dur_lin;
+__global__ void iota_kernel(int32_t* a, long long n) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+    a[k] = (int32_t)k;
+}
+
+// The model from host tables (emission given on the host, or already on the
+// device in em_dev with its max |x| in emax_dev); uploads on the thread's
+// allocation stream when set.
+int model_create_impl(int N, int O, int D, const double* trans, const double* emission, const double* em_dev,
+                      const double* start, const double* dur, tv_model* out, double emax_dev = 0.0) {
   if (!out) return fail(TV_EINVAL, "out is null");
   *out = nullptr;
   if (N <= 0 || O <= 0 || D <= 0) return fail(TV_EINVAL, "n_states, n_symbols and max_dur must be positive");
   if (N > 32768 || D > 65536) return fail(TV_ETOOBIG, "n_states must be <= 32768 and max_dur <= 65536");
-  if (!trans || !emission || !start || !dur) return fail(TV_EINVAL, "null model table");
+  if (!trans || !start || !dur || (!emission && !em_dev)) return fail(TV_EINVAL, "null model table");
   tv_model_s* m = new tv_model_s();
   m->N = N; m->O = O; m->D = D;
-  if (!all_finite(trans, (size_t)N * N, &m->tmax) || !all_finite(emission, (size_t)O * N, &m->emax) ||
-      !all_finite(start, (size_t)N, &m->smax) || !all_finite(dur, (size_t)D * N, &m->dmax)) {
+  bool ok = all_finite(trans, (size_t)N * N, &m->tmax) && all_finite(start, (size_t)N, &m->smax) &&
+            all_finite(dur, (size_t)D * N, &m->dmax);
+  if (emission) ok = ok && all_finite(emission, (size_t)O * N, &m->emax);
+  else m->emax = emax_dev;
+  if (!ok) {
     delete m;
     return fail(TV_ENONFINITE, "model tables must be finite (log(p + 1e-30) as in HSMM.to_log_space)");
   }
@@ -737,17 +806,96 @@ int tv_model_create(int N, int O, int D, const double* trans, const double* emis
     return rc;
   }
   cudaError_t e = cudaSuccess;
-  if (e == cudaSuccess) e = cudaMemcpy(m->em.p, emission, sizeof(double) * O * N, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(m->trans.p, trans, sizeof(double) * N * N, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(m->start.p, start, sizeof(double) * N, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(m->durT.p, durT.data(), sizeof(double) * N * D, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(m->survT.p, survT.data(), sizeof(double) * N * D, cudaMemcpyHostToDevice);
+  if (emission) {
+    e = upload(m->em.p, emission, sizeof(double) * O * N);
+  } else {
+    e = g_alloc_async ? cudaMemcpyAsync(m->em.p, em_dev, sizeof(double) * O * N, cudaMemcpyDeviceToDevice, g_alloc_stream)
+                      : cudaMemcpy(m->em.p, em_dev, sizeof(double) * O * N, cudaMemcpyDeviceToDevice);
+  }
+  if (e == cudaSuccess) e = upload(m->trans.p, trans, sizeof(double) * N * N);
+  if (e == cudaSuccess) e = upload(m->start.p, start, sizeof(double) * N);
+  if (e == cudaSuccess) e = upload(m->durT.p, durT.data(), sizeof(double) * N * D);
+  if (e == cudaSuccess) e = upload(m->survT.p, survT.data(), sizeof(double) * N * D);
   if (e != cudaSuccess) {
     tv_model_destroy(m);
     return fail(TV_ECUDA, std::string("model upload: ") + cudaGetErrorString(e));
   }
   *out = m;
   return TV_OK;
+}
+
+// The Gaussian front-end into a device table (T x N), on `st`.
+int gaussian_table(const double* x_dev, int64_t T, int N, const double* mean, const double* sd, double* table_dev,
+                   cudaStream_t st) {
+  if (!x_dev || !mean || !sd || !table_dev || T <= 0 || N <= 0) return fail(TV_EINVAL, "bad argument");
+  std::vector<double> par((size_t)3 * N);
+  for (int j = 0; j < N; ++j) {
+    if (!(sd[j] > 0.0) || !std::isfinite(sd[j]) || !std::isfinite(mean[j]))
+      return fail(TV_EINVAL, "Gaussian means must be finite and standard deviations positive");
+    par[j] = mean[j];
+    par[(size_t)N + j] = sd[j];
+    par[(size_t)2 * N + j] = std::log(sd[j]);
+  }
+  const double c = 0.5 * std::log(2.0 * 3.141592653589793);
+  double* par_dev = nullptr;
+  TV_CUDA(cudaMallocAsync((void**)&par_dev, sizeof(double) * 3 * N, st));
+  TV_CUDA(cudaMemcpyAsync(par_dev, par.data(), sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
+  const long long n = (long long)T * N;
+  const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
+  gaussian_loglik_kernel<<<blocks, 256, 0, st>>>(x_dev, T, N, par_dev, par_dev + N, par_dev + 2 * N, c, table_dev);
+  TV_CUDA(cudaGetLastError());
+  TV_CUDA(cudaFreeAsync(par_dev, st));
+  return TV_OK;
+}
+
+// A model whose emission table is built on the device from float64
+// observations x (host, T) and per-state Gaussian mean / sd: emission row t
+// is observation t, so the decode takes obs = 0..T-1.
+int model_create_gaussian(int N, int D, int64_t T, const double* trans, const double* start, const double* dur,
+                          const double* x, const double* mean, const double* sd, tv_model* out) {
+  if (!out) return fail(TV_EINVAL, "out is null");
+  *out = nullptr;
+  if (T <= 0 || T > 0x7fffffffLL || N <= 0) return fail(TV_EINVAL, "bad sizes");
+  if (!x || !mean || !sd) return fail(TV_EINVAL, "null Gaussian argument");
+  for (int64_t t = 0; t < T; ++t)
+    if (!std::isfinite(x[t])) return fail(TV_ENONFINITE, "observations must be finite");
+  cudaStream_t st = g_alloc_async ? g_alloc_stream : (cudaStream_t)0;
+  double* x_dev = nullptr;
+  double* table = nullptr;
+  unsigned long long* red = nullptr;
+  TV_CUDA(cudaMallocAsync((void**)&x_dev, sizeof(double) * T, st));
+  TV_CUDA(cudaMallocAsync((void**)&table, sizeof(double) * T * N, st));
+  TV_CUDA(cudaMallocAsync((void**)&red, sizeof(unsigned long long) * 2, st));
+  TV_CUDA(cudaMemcpyAsync(x_dev, x, sizeof(double) * T, cudaMemcpyHostToDevice, st));
+  int rc = gaussian_table(x_dev, T, N, mean, sd, table, st);
+  if (rc != TV_OK) return rc;
+  TV_CUDA(cudaMemsetAsync(red, 0, sizeof(unsigned long long) * 2, st));
+  absmax_kernel<<<256, 256, 0, st>>>(table, (size_t)T * N, red);
+  TV_CUDA(cudaGetLastError());
+  unsigned long long hr[2] = {0, 0};
+  TV_CUDA(cudaMemcpyAsync(hr, red, sizeof(hr), cudaMemcpyDeviceToHost, st));
+  TV_CUDA(cudaStreamSynchronize(st));
+  double emax = 0.0;
+  std::memcpy(&emax, &hr[0], sizeof(double));
+  if (hr[1]) rc = fail(TV_ENONFINITE, "the Gaussian log-likelihood table is not finite");
+  else rc = model_create_impl(N, (int)T, D, trans, nullptr, table, start, dur, out, emax);
+  cudaFreeAsync(x_dev, st);
+  cudaFreeAsync(table, st);
+  cudaFreeAsync(red, st);
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* tv_last_error(void) { return g_err.c_str(); }
+
+int tv_model_create(int N, int O, int D, const double* trans, const double* emission,
+                    const double* dur_lin, const double* start, const double* dur, tv_model* out) {
+  (void)dur_lin;
+  if (!emission) return fail(TV_EINVAL, "null model table");
+  return model_create_impl(N, O, D, trans, emission, nullptr, start, dur, out);
 }
 
 int tv_model_destroy(tv_model m) {
@@ -943,3 +1091,5 @@ int tv_decode_device_static(tv_model m, const int32_t* obs_dev, int64_t T, int32
 }
 
 }  // extern "C"
+
+#include "tv_server.cuh"

@@ -151,9 +151,15 @@ def discrete_problem(N: int, D: int, T: int, M: int, mean_lo: float = 5.0, mean_
 
 
 def gaussian_loglik_table(x: np.ndarray, mu: np.ndarray, sd: np.ndarray) -> np.ndarray:
-    """(T, N) log N(x_t; mu_j, sd_j) in float64."""
+    """(T, N) log N(x_t; mu_j, sd_j) in float64: ((-0.5 z) z - log sd_j) -
+    log(2 pi)/2 with z = (x_t - mu_j) / sd_j, each operation rounded once and
+    the logs from the C library (math.log), as the device front-end computes
+    it, so the two tables agree bit for bit."""
+    x, mu, sd = (np.asarray(a, dtype=np.float64) for a in (x, mu, sd))
+    logsd = np.array([math.log(float(v)) for v in sd], dtype=np.float64)
+    c = 0.5 * math.log(2.0 * 3.141592653589793)
     z = (x[:, None] - mu[None, :]) / sd[None, :]
-    return -0.5 * z * z - np.log(sd)[None, :] - 0.5 * math.log(2.0 * math.pi)
+    return ((-0.5 * z) * z - logsd[None, :]) - c
 
 
 def gaussian_problem(N: int, D: int, T: int, mean_lo: float = 5.0, mean_hi: float = 50.0,

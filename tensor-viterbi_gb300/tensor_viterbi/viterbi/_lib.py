@@ -52,6 +52,17 @@ EXPORTS = {
     "tv_model_kernel_ms": (C.c_double, [C.c_void_p]),
     "tv_decode_device_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p]),
+    "tv_gaussian_loglik": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, _dp, _dp, C.c_void_p, C.c_void_p]),
+    "tv_model_create_gaussian": (C.c_int, [C.c_int, C.c_int, C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                                           C.POINTER(C.c_void_p)]),
+    "tv_server_create": (C.c_void_p, [C.c_int64, C.c_int]),
+    "tv_server_destroy": (C.c_int, [C.c_void_p]),
+    "tv_server_submit": (C.c_int64, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int64, _dp, _dp, _dp, _dp, _dp, _ip]),
+    "tv_server_submit_gaussian": (C.c_int64, [C.c_void_p, C.c_int, C.c_int, C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp,
+                                              _dp]),
+    "tv_server_poll": (C.c_int, [C.c_void_p, C.c_int64, _ip, _dp, _dp]),
+    "tv_server_wait": (C.c_int, [C.c_void_p, C.c_int64, _ip, _dp, _dp]),
+    "tv_server_stats": (C.c_int, [C.c_void_p, _lp]),
 }
 
 # Size of the fixed device scratch behind tv_decode_device_static.

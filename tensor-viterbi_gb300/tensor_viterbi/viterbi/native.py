@@ -197,6 +197,129 @@ class Model:
             int(_lib.lib().tv_model_last_path(self._h)), "none")
 
 
+class GaussianModel(Model):
+    """A model whose emissions are Gaussian per state: the (T x N)
+    log-likelihood table of the float64 observations x is built on the device
+    (no reference counterpart; the reference decodes a discrete table, and the
+    same decode runs here on the per-timestep table with obs = 0..T-1)."""
+
+    def __init__(self, n_states, trans_mat, duration_probs_linear, start_probs, duration_probs, x, mean, sd):
+        L = _lib.lib()
+        N = int(n_states)
+        tm, dl, sp, dp = _f64(trans_mat), _f64(duration_probs_linear), _f64(start_probs).reshape(-1), _f64(duration_probs)
+        xs, mu, sdv = _f64(x).reshape(-1), _f64(mean).reshape(-1), _f64(sd).reshape(-1)
+        if tm.shape != (N, N) or dp.ndim != 2 or dp.shape[1] != N or dl.shape != dp.shape or sp.shape != (N,):
+            raise ValueError("[native] model table shapes do not match n_states")
+        if mu.shape != (N,) or sdv.shape != (N,):
+            raise ValueError("[native] mean and sd must have n_states entries")
+        self.N, self.O, self.D, self.T = N, xs.size, dp.shape[0], xs.size
+        h = C.c_void_p()
+        _lib.check(L.tv_model_create_gaussian(N, self.D, xs.size, _lib.dptr(tm), _lib.dptr(dl), _lib.dptr(sp),
+                                              _lib.dptr(dp), _lib.dptr(xs), _lib.dptr(mu), _lib.dptr(sdv),
+                                              C.byref(h)))
+        self._h = h
+
+    def decode(self, obs_seq=None, return_loglik: bool = False):
+        """Decode the model's own observations (emission row t = x_t)."""
+        return super().decode(np.arange(self.T, dtype=np.int32) if obs_seq is None else obs_seq, return_loglik)
+
+
+def gaussian_loglik_device(x_dev_ptr: int, T: int, mean, sd, table_dev_ptr: int, stream: int = 0) -> None:
+    """Device front-end: table (T x N, device) = log N(x_t; mean_j, sd_j) for
+    the T float64 observations at x_dev_ptr; asynchronous on `stream`."""
+    mu, sdv = _f64(mean).reshape(-1), _f64(sd).reshape(-1)
+    _lib.check(_lib.lib().tv_gaussian_loglik(C.c_void_p(x_dev_ptr), int(T), mu.size, _lib.dptr(mu), _lib.dptr(sdv),
+                                             C.c_void_p(table_dev_ptr), C.c_void_p(stream or None)))
+
+
+class Server:
+    """Decode server: continuous batching of independent requests, each with
+    its own model (no reference counterpart).  A native scheduler thread
+    admits requests in arrival order while the device-memory budget allows and
+    runs each on its own stream, so they overlap on the GPU; a result is the
+    one the request gives decoded alone.  submit()/submit_gaussian() copy the
+    inputs and return a ticket; poll() returns None while pending, else
+    (path, loglik, latency_ms, queue_ms); wait() blocks."""
+
+    def __init__(self, budget_bytes: int = 0, max_inflight: int = 64):
+        L = _lib.lib()
+        h = L.tv_server_create(int(budget_bytes), int(max_inflight))
+        if not h:
+            raise RuntimeError("[native] " + L.tv_last_error().decode(errors="replace"))
+        self._h = C.c_void_p(h)
+        self._T = {}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.lib().tv_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, n_states, trans_mat, emission_probs, duration_probs_linear, start_probs, duration_probs,
+               obs_seq) -> int:
+        N, O, D, tm, ep, dl, sp, dp = _model_arrays(
+            n_states, trans_mat, emission_probs, duration_probs_linear, start_probs, duration_probs)
+        obs = _obs_i32(obs_seq)
+        t = _lib.lib().tv_server_submit(self._h, N, O, D, obs.size, _lib.dptr(tm), _lib.dptr(ep), _lib.dptr(dl),
+                                        _lib.dptr(sp), _lib.dptr(dp), _lib.iptr(obs))
+        if t < 0:
+            _lib.check(int(t))
+        self._T[t] = obs.size
+        return int(t)
+
+    def submit_gaussian(self, n_states, trans_mat, duration_probs_linear, start_probs, duration_probs, x, mean,
+                        sd) -> int:
+        N = int(n_states)
+        tm, dl, sp, dp = _f64(trans_mat), _f64(duration_probs_linear), _f64(start_probs).reshape(-1), _f64(duration_probs)
+        xs, mu, sdv = _f64(x).reshape(-1), _f64(mean).reshape(-1), _f64(sd).reshape(-1)
+        if tm.shape != (N, N) or dp.ndim != 2 or dp.shape[1] != N or mu.shape != (N,) or sdv.shape != (N,):
+            raise ValueError("[native] Gaussian request shapes do not match n_states")
+        t = _lib.lib().tv_server_submit_gaussian(self._h, N, dp.shape[0], xs.size, _lib.dptr(tm), _lib.dptr(dl),
+                                                 _lib.dptr(sp), _lib.dptr(dp), _lib.dptr(xs), _lib.dptr(mu),
+                                                 _lib.dptr(sdv))
+        if t < 0:
+            _lib.check(int(t))
+        self._T[t] = xs.size
+        return int(t)
+
+    def _take(self, ticket: int, block: bool):
+        T = self._T[ticket]
+        path = np.empty(T, dtype=np.int32)
+        ll = np.zeros(1, dtype=np.float64)
+        lat = np.zeros(2, dtype=np.float64)
+        fn = _lib.lib().tv_server_wait if block else _lib.lib().tv_server_poll
+        rc = fn(self._h, int(ticket), _lib.iptr(path), _lib.dptr(ll), _lib.dptr(lat))
+        if rc == 0:
+            return None
+        del self._T[ticket]
+        if rc < 0:
+            _lib.check(rc)
+        return path, float(ll[0]), float(lat[0]), float(lat[1])
+
+    def poll(self, ticket: int):
+        return self._take(ticket, False)
+
+    def wait(self, ticket: int):
+        return self._take(ticket, True)
+
+    def stats(self) -> dict:
+        out = np.zeros(8, dtype=np.int64)
+        _lib.check(_lib.lib().tv_server_stats(self._h, _lib.lptr(out)))
+        keys = ["admitted", "completed", "failed", "running", "pending", "bytes_in_use", "peak_bytes", "budget"]
+        return dict(zip(keys, map(int, out)))
+
+
 def decode_tensor_viterbi_cuda_loglik(n_states, trans_mat, emission_probs, duration_probs_linear,
                                       start_probs, duration_probs, obs_seq):
     """Like decode_tensor_viterbi_cuda, also returning the path log-likelihood."""
