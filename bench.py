@@ -52,6 +52,12 @@ WORKLOADS = {
     "single_N100_D10000_T1e7": dict(N=100, D=10_000, T=10_000_000, M=64, lo=5.0, hi=50.0, seed=4),
     # 4096 sequences sharing one model, lengths log-uniform in [1e3, 1e5]
     "batch_4096_N10_D250": dict(kind="batch", n_seq=4096, N=10, D=250, M=16, lo=1e3, hi=1e5, seed=2),
+    # served: Poisson arrivals of requests with their own models; N from
+    # {10,15,25,50}, D from {100,250,500,1000}, T log-uniform in [1e3, 1e6],
+    # half discrete (M = 32), half Gaussian; three arrival rates
+    "served_N10-50_D100-1000_T1e3-1e6": dict(kind="served", n_req=1000, Ns=[10, 15, 25, 50], Ds=[100, 250, 500, 1000],
+                                             Tlo=1e3, Thi=1e6, M=32, lo=5.0, hi=50.0, rates=[50.0, 200.0, 800.0],
+                                             seed=3),
 }
 
 
@@ -307,6 +313,153 @@ def run_ours(args, w, wname):
     return 0
 
 
+def served_requests(w):
+    """The served workload's requests: (kind, problem) with each request's own
+    seeded model; observations sampled from it."""
+    import bisect
+    import math
+    import numpy as np
+    import tensor_viterbi.synthetic as syn
+    rng = np.random.default_rng(w["seed"])
+    reqs = []
+    for k in range(w["n_req"]):
+        N = int(rng.choice(w["Ns"]))
+        D = int(rng.choice(w["Ds"]))
+        T = int(math.exp(rng.uniform(math.log(w["Tlo"]), math.log(w["Thi"]))))
+        T = max(T, D)
+        gauss = k % 2 == 1
+        lm = syn.random_model(rng, N, D, 2 if gauss else w["M"], w["lo"], w["hi"])
+        # segment-wise state path (bisect on cumulative rows: fast per segment)
+        cP = [list(np.cumsum(r) / r.sum()) for r in lm.P]
+        cA = [list(np.cumsum(r) / r.sum()) for r in lm.A]
+        cpi = list(np.cumsum(lm.pi) / lm.pi.sum())
+        u = rng.random(2 * T + 2).tolist()
+        states = np.empty(T, dtype=np.int32)
+        t, ui = 0, 0
+        s_ = min(bisect.bisect_right(cpi, u[ui]), N - 1)
+        ui += 1
+        while t < T:
+            dlen = min(bisect.bisect_right(cP[s_], u[ui]), D - 1) + 1
+            states[t:t + dlen] = s_
+            t += dlen
+            s_ = min(bisect.bisect_right(cA[s_], u[ui + 1]), N - 1)
+            ui += 2
+        if gauss:
+            mu = rng.normal(0.0, 2.0, size=N)
+            sd = rng.uniform(0.5, 2.0, size=N)
+            x = rng.normal(mu[states], sd[states])
+            p = syn.to_problem(lm, np.zeros(0, dtype=np.int32), emission_log=np.zeros((1, N)),
+                               meta=dict(x=x, mu=mu, sd=sd))
+            reqs.append(("gauss", p, T))
+        else:
+            obs = syn.sample_discrete_obs(rng, lm.B, states)
+            reqs.append(("disc", syn.to_problem(lm, obs), T))
+    return reqs
+
+
+def run_served(args, w, wname):
+    """Served decode: Poisson arrivals into the decode server at several
+    rates; latency from submission to completion (server clock), throughput
+    over the makespan; and the plain per-request loop on a sample."""
+    import random
+    import threading
+    import numpy as np
+    from tensor_viterbi.viterbi import native
+    native.configure("gb300", "cuda")
+    reqs = served_requests(w)
+    cells = [T * p.n_states * p.D for _, p, T in reqs]
+
+    def submit(srv, kind, p):
+        if kind == "disc":
+            return srv.submit(*p.args())
+        return srv.submit_gaussian(p.n_states, p.trans_mat, p.duration_probs_linear, p.start_probs,
+                                   p.duration_probs, p.meta["x"], p.meta["mu"], p.meta["sd"])
+
+    # plain loop: the same kind of requests decoded one at a time (a sample)
+    sample = reqs[8:8 + 24]
+
+    def plain(k, p):
+        if k == "disc":
+            with native.Model(*p.model_args()) as m:
+                m.decode(p.obs_seq)
+        else:
+            with native.GaussianModel(p.n_states, p.trans_mat, p.duration_probs_linear, p.start_probs,
+                                      p.duration_probs, p.meta["x"], p.meta["mu"], p.meta["sd"]) as m:
+                m.decode()
+
+    plain(*reqs[0][:2])  # warm-up (context, kernel loading)
+    t0 = time.perf_counter()
+    for k, p, _ in sample:
+        if k == "disc":
+            with native.Model(*p.model_args()) as m:
+                m.decode(p.obs_seq)
+        else:
+            with native.GaussianModel(p.n_states, p.trans_mat, p.duration_probs_linear, p.start_probs,
+                                      p.duration_probs, p.meta["x"], p.meta["mu"], p.meta["sd"]) as m:
+                m.decode()
+    loop_rate = sum(T * p.n_states * p.D for _, p, T in sample) / (time.perf_counter() - t0)
+    # warm-up: a few requests through a server (kernel loading, pool growth)
+    with native.Server() as srv:
+        for t in [submit(srv, k, p) for k, p, _ in reqs[:8]]:
+            srv.wait(t)
+    out = []
+    clocks = None
+    for rate in (w["rates"] if not args.rates else [float(r) for r in args.rates.split(",")]):
+        rnd = random.Random(int(rate) * 7919 + w["seed"])
+        arrivals, acc = [], 0.0
+        for _ in reqs:
+            acc += rnd.expovariate(rate)
+            arrivals.append(acc)
+        with native.Server() as srv:
+            tickets = [None] * len(reqs)
+            t0 = time.perf_counter()
+
+            def feeder():
+                for i, (k, p, _) in enumerate(reqs):
+                    dt = arrivals[i] - (time.perf_counter() - t0)
+                    if dt > 0:
+                        time.sleep(dt)
+                    tickets[i] = submit(srv, k, p)
+
+            th = threading.Thread(target=feeder)
+            if clocks is None:
+                import torch
+                clocks = ClockSampler(torch.cuda.current_device())
+                clocks.start()
+            th.start()
+            lat, queue, errors = [], [], []
+            for i in range(len(reqs)):
+                while tickets[i] is None:
+                    time.sleep(0.0005)
+                try:
+                    _, _, l_ms, q_ms = srv.wait(tickets[i])
+                except RuntimeError as e:
+                    k, p, T = reqs[i]
+                    errors.append(f"{k} N={p.n_states} D={p.D} T={T}: {e} stats={srv.stats()}")
+                    continue
+                lat.append(l_ms)
+                queue.append(q_ms)
+            th.join()
+            makespan = time.perf_counter() - t0
+            st = srv.stats()
+        out.append({"rate_per_s": rate, "requests": len(reqs), "p50_ms": float(np.percentile(lat, 50)),
+                    "p99_ms": float(np.percentile(lat, 99)), "mean_queue_ms": float(np.mean(queue)),
+                    "throughput_cells_per_s": sum(cells) / makespan, "makespan_s": makespan,
+                    "completed": st["completed"], "failed": st["failed"], "peak_bytes": st["peak_bytes"],
+                    "budget_bytes": st["budget"], "errors": errors[:3]})
+    clk = clocks.stop() if clocks else None
+    best = max(r["throughput_cells_per_s"] for r in out)
+    line = {"metric": "served decode: p50/p99 latency and cells/s at Poisson arrival rates", "value": best,
+            "unit": "cells/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wname, "requests_per_rate": len(reqs), "N": w["Ns"], "D": w["Ds"],
+                       "T": f"log-uniform [{w['Tlo']:g}, {w['Thi']:g}]", "emissions": "half discrete (M=32), half Gaussian",
+                       "form": "served (continuous batching)"},
+            "rates": out, "plain_loop_cells_per_s": loop_rate, "vs_plain_loop": best / loop_rate,
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_batch(args, w, wname):
     """Batched form: all sequences in one persistent launch, against the plain
     single-sequence decode looped over a sample of the same sequences."""
@@ -480,10 +633,19 @@ def main():
     ap.add_argument("--no-e2e", action="store_true",
                     help="skip the host-buffer (drop-in call) measurement: long stress workloads")
     ap.add_argument("--T", type=int, default=0, help="override the sequence length (profiling runs)")
+    ap.add_argument("--rates", default="", help="served workload: comma-separated arrival rates (per s)")
+    ap.add_argument("--requests", type=int, default=0, help="served workload: number of requests per rate")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload])
     if args.T:
         w["T"] = args.T
+    if args.requests:
+        w["n_req"] = args.requests
+    if w.get("kind") == "served":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no served form; its arm is measured on the single-sequence workload"}))
+            return 0
+        return run_served(args, w, args.workload)
     if w.get("kind") == "batch":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm is measured on the single-sequence workload"}))

@@ -54,6 +54,10 @@ struct DevBuf {
   size_t n = 0;
   cudaStream_t st = nullptr;  // stream-ordered buffer: its stream
   bool async = false;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
   int ensure(size_t count) {
     if (count <= n && p) return TV_OK;
     release();
@@ -65,10 +69,22 @@ struct DevBuf {
       async = true;
     } else {
       e = cudaMalloc(&p, count * sizeof(T));
+      if (e == cudaErrorMemoryAllocation) {
+        // memory a stream-ordered pool keeps for reuse: give it back, retry once
+        cudaGetLastError();
+        int dev = 0;
+        cudaMemPool_t pool;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+          cudaDeviceSynchronize();
+          cudaMemPoolTrimTo(pool, 0);
+          e = cudaMalloc(&p, count * sizeof(T));
+        }
+      }
       async = false;
     }
     if (e != cudaSuccess) {
       p = nullptr;
+      cudaGetLastError();  // an allocation failure is not sticky; do not let it resurface later
       return fail(TV_ENOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
     }
     n = count;
@@ -863,25 +879,40 @@ int model_create_gaussian(int N, int D, int64_t T, const double* trans, const do
   double* x_dev = nullptr;
   double* table = nullptr;
   unsigned long long* red = nullptr;
-  TV_CUDA(cudaMallocAsync((void**)&x_dev, sizeof(double) * T, st));
-  TV_CUDA(cudaMallocAsync((void**)&table, sizeof(double) * T * N, st));
-  TV_CUDA(cudaMallocAsync((void**)&red, sizeof(unsigned long long) * 2, st));
-  TV_CUDA(cudaMemcpyAsync(x_dev, x, sizeof(double) * T, cudaMemcpyHostToDevice, st));
-  int rc = gaussian_table(x_dev, T, N, mean, sd, table, st);
-  if (rc != TV_OK) return rc;
-  TV_CUDA(cudaMemsetAsync(red, 0, sizeof(unsigned long long) * 2, st));
-  absmax_kernel<<<256, 256, 0, st>>>(table, (size_t)T * N, red);
-  TV_CUDA(cudaGetLastError());
+  auto cleanup = [&]() {
+    if (x_dev) cudaFreeAsync(x_dev, st);
+    if (table) cudaFreeAsync(table, st);
+    if (red) cudaFreeAsync(red, st);
+  };
+  cudaError_t e = cudaMallocAsync((void**)&x_dev, sizeof(double) * T, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&table, sizeof(double) * T * N, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&red, sizeof(unsigned long long) * 2, st);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    cleanup();
+    return fail(TV_ENOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
+  }
+  e = cudaMemcpyAsync(x_dev, x, sizeof(double) * T, cudaMemcpyHostToDevice, st);
+  int rc = e == cudaSuccess ? gaussian_table(x_dev, T, N, mean, sd, table, st)
+                            : fail(TV_ECUDA, std::string("upload: ") + cudaGetErrorString(e));
   unsigned long long hr[2] = {0, 0};
-  TV_CUDA(cudaMemcpyAsync(hr, red, sizeof(hr), cudaMemcpyDeviceToHost, st));
-  TV_CUDA(cudaStreamSynchronize(st));
-  double emax = 0.0;
-  std::memcpy(&emax, &hr[0], sizeof(double));
-  if (hr[1]) rc = fail(TV_ENONFINITE, "the Gaussian log-likelihood table is not finite");
-  else rc = model_create_impl(N, (int)T, D, trans, nullptr, table, start, dur, out, emax);
-  cudaFreeAsync(x_dev, st);
-  cudaFreeAsync(table, st);
-  cudaFreeAsync(red, st);
+  if (rc == TV_OK) {
+    e = cudaMemsetAsync(red, 0, sizeof(unsigned long long) * 2, st);
+    if (e == cudaSuccess) {
+      absmax_kernel<<<256, 256, 0, st>>>(table, (size_t)T * N, red);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hr, red, sizeof(hr), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = fail(TV_ECUDA, std::string("Gaussian front-end: ") + cudaGetErrorString(e));
+  }
+  if (rc == TV_OK) {
+    double emax = 0.0;
+    std::memcpy(&emax, &hr[0], sizeof(double));
+    if (hr[1]) rc = fail(TV_ENONFINITE, "the Gaussian log-likelihood table is not finite");
+    else rc = model_create_impl(N, (int)T, D, trans, nullptr, table, start, dur, out, emax);
+  }
+  cleanup();
   return rc;
 }
 
@@ -903,7 +934,7 @@ int tv_model_destroy(tv_model m) {
   m->em.release(); m->trans.release(); m->start.release(); m->durT.release(); m->survT.release();
   m->qem.release(); m->qtr.release(); m->qdurT.release();
   m->psi.release(); m->status.release(); m->counter.release(); m->off.release(); m->order.release(); m->scratch.release();
-  m->msgs.release(); m->dinit.release(); m->ck.release(); m->wrange.release();
+  m->msgs.release(); m->dinit.release(); m->ck.release(); m->hwin.release(); m->wrange.release(); m->wglob.release();
   m->seg_first.release(); m->seg_count.release(); m->seg_base.release(); m->gflags.release();
   if (m->ev0) cudaEventDestroy(m->ev0);
   if (m->ev1) cudaEventDestroy(m->ev1);

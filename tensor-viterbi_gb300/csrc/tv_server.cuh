@@ -102,6 +102,8 @@ struct tv_server_s {
   std::vector<int> free_slots;
   std::thread th;
   bool stop = false;
+  bool hold = false;  // admission paused until the next completion
+  uint64_t pool_keep_before = 0;  // the pool's retention setting before this server
   int dev = 0, smem_optin = 0;
   std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
 
@@ -137,7 +139,10 @@ struct tv_server_s {
           e = cudaMemcpyAsync(r->obs_dev, r->obs.data(), sizeof(int32_t) * r->T, cudaMemcpyHostToDevice, r->st);
         }
       }
-      if (e != cudaSuccess) rc = fail(TV_ENOMEM, std::string("request buffers: ") + cudaGetErrorString(e));
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        rc = fail(TV_ENOMEM, std::string("request buffers: ") + cudaGetErrorString(e));
+      }
     }
     if (rc == TV_OK) {
       std::lock_guard<std::mutex> lk(r->m->mu);
@@ -149,6 +154,20 @@ struct tv_server_s {
       r->error = g_err;
     }
     cudaEventRecord(r->ev, r->st);
+    g_alloc_async = false;
+  }
+
+  // Frees a request's device memory (in its stream's order).
+  void release_request(SrvRequest* r) {
+    g_alloc_async = true;
+    g_alloc_stream = r->st;
+    if (r->obs_dev) cudaFreeAsync(r->obs_dev, r->st);
+    if (r->path_dev) cudaFreeAsync(r->path_dev, r->st);
+    if (r->ll_dev) cudaFreeAsync(r->ll_dev, r->st);
+    r->obs_dev = r->path_dev = nullptr;
+    r->ll_dev = nullptr;
+    if (r->m) tv_model_destroy(r->m);
+    r->m = nullptr;
     g_alloc_async = false;
   }
 
@@ -169,14 +188,8 @@ struct tv_server_s {
         r->error = g_err;
       }
     }
-    if (r->obs_dev) cudaFreeAsync(r->obs_dev, r->st);
-    if (r->path_dev) cudaFreeAsync(r->path_dev, r->st);
-    if (r->ll_dev) cudaFreeAsync(r->ll_dev, r->st);
-    r->obs_dev = r->path_dev = nullptr;
-    r->ll_dev = nullptr;
-    if (r->m) tv_model_destroy(r->m);
-    r->m = nullptr;
     g_alloc_async = false;
+    release_request(r);
     // free the inputs; keep the results
     std::vector<double>().swap(r->trans); std::vector<double>().swap(r->em); std::vector<double>().swap(r->x);
     std::vector<int32_t>().swap(r->obs);
@@ -195,8 +208,9 @@ struct tv_server_s {
           continue;
         }
         // admission in arrival order while memory and a stream allow (a
-        // request alone on an idle device is always admitted)
-        while (!pending.empty() && !free_slots.empty()) {
+        // request alone on an idle device is always admitted); after a
+        // placement failure, wait for a completion first
+        while (!hold && !pending.empty() && !free_slots.empty()) {
           SrvRequest* r = pending.front();
           const bool big = tv::make_cta_layout(r->N, r->D).bytes + 64 > (size_t)smem_optin;
           const size_t need = request_bytes(*r, big, 16);
@@ -214,9 +228,43 @@ struct tv_server_s {
           to_start.push_back(r);
         }
       }
-      for (SrvRequest* r : to_start) {
+      for (size_t q = 0; q < to_start.size(); ++q) {
+        SrvRequest* r = to_start[q];
         start_request(r);
         std::lock_guard<std::mutex> lk(mu);
+        if (r->status == TV_ENOMEM && !running.empty()) {
+          // The estimate let it in but the device could not place it (the
+          // pool's free blocks are fragmented): give the memory back, trim
+          // the pool and retry it first once another request completes.
+          cudaStreamSynchronize(r->st);
+          release_request(r);
+          cudaStreamSynchronize(r->st);
+          cudaMemPool_t pool;
+          if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
+          r->status = TV_OK;
+          r->error.clear();
+          in_use -= r->bytes;
+          for (size_t s2 = 0; s2 < streams.size(); ++s2)
+            if (streams[s2] == r->st) free_slots.push_back((int)s2);
+          r->st = nullptr;
+          r->ev = nullptr;
+          --admitted;
+          // this one and the rest of this round go back in arrival order
+          for (size_t q2 = to_start.size(); q2-- > q + 1;) {
+            SrvRequest* o = to_start[q2];
+            in_use -= o->bytes;
+            for (size_t s2 = 0; s2 < streams.size(); ++s2)
+              if (streams[s2] == o->st) free_slots.push_back((int)s2);
+            o->st = nullptr;
+            o->ev = nullptr;
+            --admitted;
+            pending.push_front(o);
+          }
+          pending.push_front(r);
+          hold = true;
+          progress = true;
+          break;
+        }
         running.push_back(r);
         progress = true;
       }
@@ -249,7 +297,10 @@ struct tv_server_s {
         else ++failed;
         progress = true;
       }
-      if (!done_now.empty()) cv.notify_all();
+      if (!done_now.empty()) {
+        hold = false;
+        cv.notify_all();
+      }
       if (!progress) std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
   }
@@ -270,11 +321,13 @@ tv_server tv_server_create(int64_t budget_bytes, int max_inflight) {
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
   s->budget = budget_bytes > 0 ? (size_t)budget_bytes : (size_t)(0.8 * (double)free_b);
-  // Keep freed pool memory for reuse instead of returning it at each
-  // synchronisation (a property of this process's pool).
+  // Keep part of the freed pool memory for reuse instead of returning it at
+  // each synchronisation (a property of this process's pool); the rest goes
+  // back, which bounds fragmentation.
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, s->dev) == cudaSuccess) {
-    uint64_t keep = s->budget;
+    cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &s->pool_keep_before);
+    uint64_t keep = s->budget / 4;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
   for (int k = 0; k < max_inflight; ++k) {
@@ -309,8 +362,17 @@ int tv_server_destroy(tv_server s) {
   s->cv.notify_all();
   if (s->th.joinable()) s->th.join();
   for (auto& kv : s->finished) delete kv.second;
-  for (cudaStream_t st : s->streams) cudaStreamDestroy(st);
+  for (cudaStream_t st : s->streams) {
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+  }
   for (cudaEvent_t ev : s->events) cudaEventDestroy(ev);
+  // hand the pool's memory back and restore its retention setting
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, s->dev) == cudaSuccess) {
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &s->pool_keep_before);
+    cudaMemPoolTrimTo(pool, 0);
+  }
   delete s;
   return TV_OK;
 }

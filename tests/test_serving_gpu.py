@@ -137,3 +137,35 @@ def test_server_rejects_bad_requests_at_submission(tvlib):
         path, ll, _, _ = srv.wait(t)
     ref = orc.decode(*q.args())
     np.testing.assert_array_equal(path, ref["path"])
+
+
+def test_models_return_all_device_memory(tvlib):
+    """Creating, using and destroying models (grid path, window in shared
+    memory and in L2, and the Gaussian front-end) leaves the device's free
+    memory where it was."""
+    import gc
+    import torch
+    import tensor_viterbi.synthetic as syn
+    p = syn.discrete_problem(20, 600, 30000, 16, 20.0, 300.0, seed=9)
+    g = _gauss(15, 500, 20000, seed=10, lo=20.0, hi=300.0)
+
+    def churn():
+        for kind in ("grid", "grid-l2"):
+            with tvlib.Model(*p.model_args()) as m:
+                m.set_path(kind, 0)
+                m.decode(p.obs_seq)
+        with tvlib.GaussianModel(g.n_states, g.trans_mat, g.duration_probs_linear, g.start_probs,
+                                 g.duration_probs, g.meta["x"], g.meta["mu"], g.meta["sd"]) as m:
+            m.decode()
+
+    churn()  # first use: context and module state
+    torch.cuda.synchronize()
+    gc.collect()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        churn()
+    torch.cuda.synchronize()
+    gc.collect()
+    free1, _ = torch.cuda.mem_get_info()
+    # each churn allocates well over 100 MB (window-sum table, back-pointers)
+    assert free0 - free1 < 32 << 20, (free0, free1)
