@@ -478,15 +478,9 @@ def run_batch(args, w, wname):
     native.configure("gb300", "cuda")
     prob, seqs = syn.batch_problem(w["n_seq"], w["N"], w["D"], w["M"], w["lo"], w["hi"], seed=w["seed"])
     # ranks take a longest-processing-time share of the sequences (no collective)
-    order = np.argsort([-s.size for s in seqs], kind="stable")
-    loads = np.zeros(ws)
-    mine = []
-    for k in order:
-        r = int(np.argmin(loads))
-        loads[r] += seqs[k].size
-        if r == rank:
-            mine.append(int(k))
-    my = [seqs[k] for k in sorted(mine)]
+    from tensor_viterbi.sharding import my_shard
+    mine = my_shard([s.size for s in seqs], ws, rank)
+    my = [seqs[k] for k in mine]
     N, D = w["N"], w["D"]
     lens = np.array([s.size for s in my], dtype=np.int64)
     cells = int(lens.sum()) * N * D
