@@ -40,8 +40,9 @@
 namespace tv {
 
 constexpr int GRID_THREADS = 640;    // largest block (96 registers a thread)
-constexpr int WORKER_THREADS = 256;     // a worker CTA keeps 8 warps (window in shared memory); the rest exit
+constexpr int WORKER_THREADS = 256;     // a worker CTA's scan threads: 8 warps (window in shared memory)
 constexpr int WORKER_THREADS_GW = 512;  // 16 warps when the window is in global memory (more loads in flight)
+constexpr int WORKER_SERVICE = 64;      // + a certify warp and an intake warp; the rest of the CTA exits
 constexpr int GRID_L = 8;            // head candidates d < L (a power of two)
 constexpr int CK_STRIDE = 32;      // checkpoint stride of the early window sums
 constexpr int PART_RING = 32;      // steps of worker partials in flight
@@ -58,7 +59,7 @@ struct GridParams {
   int G, L, S, Rd, M;
   long long chunk;  // largest worker range, in cells
   int max_seg;
-  unsigned long long w_qd, w_dur, w_tr, w_ctil, w_dsel, w_acc0, w_acc1, w_itil, w_red, w_emw, w_bytes;
+  unsigned long long w_qd, w_dur, w_tr, w_ctil, w_dsel, w_acc, w_accs, w_itil, w_red, w_emw, w_bytes;
   int w_global;                  // the window lives in global memory (L2), not in shared memory
   unsigned long long w_gstride;  // bytes of one worker's window in global memory
   // head shared-memory offsets
@@ -67,9 +68,9 @@ struct GridParams {
   int trans_smem;     // the exact transition matrix is kept in the head's shared memory
   int qtr_smem;       // so is its fixed-point copy (else computed from the exact one)
   int cs_dense;       // critical threads of the dense (one lane per state) phase: N rounded up to 32
-  int st_threads;     // state helper threads: N rounded up to 32
-  int in_threads;     // intake threads: S rounded up to 32
-  int block;          // threads per CTA: the head's roles (at least WORKER_THREADS)
+  int st_threads;     // state helper threads per group (two groups): N rounded up to 32
+  int in_threads;     // intake threads: max(ceil(S/2), N) rounded up to 32
+  int block;          // threads per CTA: the head's roles (at least a worker's scan and service threads)
   int head_group;     // matvec lanes per state in the head (4, or 2 for large N)
   int qf;             // fraction bits of the fixed-point scores
   int Np;             // N rounded up to 16 (packed coarse matvec rows)
@@ -193,11 +194,42 @@ __global__ void grid_prep_ck(ModelView m, const int32_t* obs, double* ck, int M,
 
 // Wait sites reported with a timeout.
 enum { SITE_HEAD_PARTIAL = 1, SITE_WORKER_SLOT = 2, SITE_WORKER_RESCORE = 3, SITE_WORKER_TAIL = 4,
-       SITE_HEAD_TAIL = 5 };
+       SITE_HEAD_TAIL = 5, SITE_HEAD_COPY = 6 };
 
 __device__ __forceinline__ void grid_fail(const GridBufs& B, int code, int site) {
   if (atomicCAS(B.status, 0, code) == 0) *B.site = site;
   atomicExch(B.abort_flag, 1);
+}
+
+// A slot message (score, selected delta, argmax word) in one round trip:
+// the five words are loaded together and polled until each carries `tag`.
+__device__ __forceinline__ bool slot_load(const unsigned long long* src, unsigned tag, unsigned long long& cbits,
+                                          unsigned long long& dbits, unsigned& ibits, const int* abort_flag,
+                                          long long limit) {
+  unsigned long long w[SLOT_WORDS];
+#pragma unroll
+  for (int k = 0; k < SLOT_WORDS; ++k) w[k] = ld_relaxed_u64(src + k);
+  auto ready = [&]() {
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < SLOT_WORDS; ++k) ok = ok && (unsigned)(w[k] >> 32) == tag;
+    return ok;
+  };
+  if (!ready()) {
+    const long long t0 = clock64();
+    for (;;) {
+      __nanosleep(20);
+#pragma unroll
+      for (int k = 0; k < SLOT_WORDS; ++k) w[k] = ld_relaxed_u64(src + k);
+      if (ready()) break;
+      if (ld_relaxed_i32(abort_flag)) return false;
+      if (clock64() - t0 > limit) return false;
+    }
+  }
+  cbits = (w[0] & 0xffffffffull) | ((w[1] & 0xffffffffull) << 32);
+  dbits = (w[2] & 0xffffffffull) | ((w[3] & 0xffffffffull) << 32);
+  ibits = (unsigned)(w[4] & 0xffffffffull);
+  return true;
 }
 
 // Exact delta[s][i] from the tagged ring (tag s+1), as an order key.
@@ -210,13 +242,18 @@ __device__ __forceinline__ bool load_dstar(const GridBufs& B, const GridParams& 
   return true;
 }
 
-// Named barrier of the worker threads only (the rest of the CTA has exited).
-// The non-aligned barrier counts threads, so lanes of a warp may arrive apart
+// Named barriers of a worker CTA: 1 for its scan threads, 2 for the scan
+// threads with the service warps (the rest of the CTA has exited).  The
+// non-aligned barrier counts threads, so lanes of a warp may arrive apart
 // (after a lane-0 wait, say); the aligned bar.sync would need the warp
 // converged, which the compiler does not ensure before inline assembly.
 template <int WT>
 __device__ __forceinline__ void worker_sync() {
   asm volatile("barrier.sync 1, %0;" ::"r"(WT) : "memory");
+}
+template <int WT>
+__device__ __forceinline__ void worker_sync_all() {
+  asm volatile("barrier.sync 2, %0;" ::"r"(WT + WORKER_SERVICE) : "memory");
 }
 
 // Block-wide reduction of an ExactBest over the worker threads; every worker
@@ -244,7 +281,18 @@ __device__ __forceinline__ void send_partial(const GridBufs& B, const GridParams
 }
 
 // ---------------------------------------------------------------------------
-// Worker CTA (WORKER_THREADS threads, WORKER_THREADS_GW with the window in global memory)
+// Worker CTA: WORKER_THREADS scan threads (WORKER_THREADS_GW with the window
+// in global memory) and two service warps, run as a software pipeline.
+// Step t:
+//   scan threads   phase 1: the fixed-point scan of the worker's cells over
+//                  d in [L, tau) (best and runner-up per segment), fused with
+//                  the exact window folds of step t+1;
+//   certify warp   (during phase 1 of step t+1) the certified exact winner of
+//                  each segment at step t, sent to the head;
+//   intake warp    (during phase 1 of step t+1) the slot that enters the scan
+//                  at step t+2 (s' = t+1-L, d = L then), from the head.
+// So the window sums are kept in three buffers (E_t, E_{t+1}, E_{t+2}) and the
+// per-warp scan results in two (by step parity).
 // ---------------------------------------------------------------------------
 // GW: the worker's window (slot scores, selected deltas, window sums, argmax
 // words) lives in a private global-memory buffer, served by L1/L2, and the
@@ -255,6 +303,7 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
   constexpr int L = GRID_L;
   constexpr int WT = GW ? WORKER_THREADS_GW : WORKER_THREADS;
   constexpr int NW = WT / 32;
+  static_assert(NW <= 32 && (32 % NW) == 0, "segment groups of the certify warp");
   const int N = m.N, D = m.D;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int w = blockIdx.x - 1;
@@ -274,23 +323,26 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
   const double* tr = GW ? m.trans + (size_t)ja * N : tr_s;
   long long* ctil = (long long*)(wb + P.w_ctil);      // [ncell]
   double* dsel = (double*)(wb + P.w_dsel);            // [ncell]
-  double* acc_cur = (double*)(wb + P.w_acc0);         // [ncell] E_t
-  double* acc_nxt = (double*)(wb + P.w_acc1);         // [ncell] E_{t+1}
+  double* accb = (double*)(wb + P.w_acc);             // [3][ncell] E_t in buffer t % 3
+  const size_t accs = P.w_accs / sizeof(double);
   unsigned short* itil = (unsigned short*)(wb + P.w_itil);
-  Top2* red = (Top2*)(sm + P.w_red);                  // [nseg][NW]
+  Top2* red = (Top2*)(sm + P.w_red);                  // [2][nseg][NW] by step parity
   ExactBest* ered = (ExactBest*)(sm + P.w_red);
   double* emw = (double*)(sm + P.w_emw);              // [2][max_seg] emission of the fold's step
-  __shared__ int s_bad;
+  // Failure flags by step parity: set by the service warps of step t, read
+  // by every thread after the barrier that ends their work, so that all
+  // leave at the same step.
+  __shared__ int s_bad[2];
+  const bool is_scan = tid < WT;
 
-  if (!GW) {
+  if (is_scan && !GW) {
     for (long long k = tid; k < (long long)nseg * D; k += WT) {
       qd_s[k] = m.qdurT[(size_t)ja * D + k];
       dur_s[k] = m.durT[(size_t)ja * D + k];
     }
     for (int k = tid; k < nseg * N; k += WT) tr_s[k] = m.trans[(size_t)ja * N + k];
   }
-  if (tid == 0) s_bad = 0;
-  worker_sync<WT>();
+  if (tid == 0) { s_bad[0] = 0; s_bad[1] = 0; }
 
   auto seg_of = [&](int s, int& rb, int& re) {
     rb = (s == 0) ? off0 : 0;
@@ -308,170 +360,193 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
     if (3 < T) em_pf = m.em[(size_t)B.obs[3] * N + j];
     if (4 < T) ob_pf = B.obs[4];
   }
-  worker_sync<WT>();
+  worker_sync_all<WT>();
 
   int r0 = 0;  // (t-1) % D
-  for (long long t = 1; t < T; ++t) {
-    const int tau = (int)(t < D ? t : D);
-    const unsigned prow = (unsigned)t & (PART_RING - 1);
-    const long long t1 = t + 1;
-    int r0n = r0 + 1;  // t % D: the slot that enters at step t+1 (d = 0 then)
-    if (r0n == D) r0n = 0;
-    if (tid < nseg) {
-      if (t + 2 < T) emw[(int)((t + 2) & 1) * P.max_seg + tid] = em_pf;
-      if (t + 3 < T) em_pf = m.em[(size_t)ob_pf * N + ja + tid];
-      if (t + 4 < T) ob_pf = B.obs[t + 4];
-    }
+  int a3 = 1;  // t % 3: the buffer of E_t
+  if (is_scan) {
+    for (long long t = 1; t < T; ++t) {
+      const int tau = (int)(t < D ? t : D);
+      const long long t1 = t + 1;
+      int r0n = r0 + 1;  // t % D: the slot that enters at step t+1 (d = 0 then)
+      if (r0n == D) r0n = 0;
+      const int an3 = a3 == 2 ? 0 : a3 + 1;  // (t+1) % 3
+      if (tid < nseg) {
+        if (t + 2 < T) emw[(int)((t + 2) & 1) * P.max_seg + tid] = em_pf;
+        if (t + 3 < T) em_pf = m.em[(size_t)ob_pf * N + ja + tid];
+        if (t + 4 < T) ob_pf = B.obs[t + 4];
+      }
 
-    // Phase 1: fixed-point scan over d in [L, tau), fused with the exact
-    // window folds of step t+1 into the other buffer (src/hsmm.cu:298-310):
-    // E_{t+1}[d] = E_t[d-1] + em_{t+1}, E_{t+1}[0] = 0 + em_{t+1}.  The FP64
-    // adds overlap the integer scan.
-    const bool fold = (t1 < T) && (t1 > D + 1);
-    for (int s = 0; s < nseg; ++s) {
-      int rb, re;
-      seg_of(s, rb, re);
-      const long long* ct = ctil + s * D - off0;
-      const long long* q = qd + s * D;
-      const double* ac = acc_cur + s * D - off0;
-      double* an = acc_nxt + s * D - off0;
-      const double em1 = fold ? emw[(int)(t1 & 1) * P.max_seg + s] : 0.0;
-      Top2 tb;
-      tb.init();
-#pragma unroll 4
-      for (int r = rb + tid; r < re; r += WT) {
-        int d = r0 - r;
-        if (d < 0) d += D;
-        if (d >= L && d < tau) tb.push(ct[r] + q[d], d);
-        if (fold) an[r] = ((r == r0n) ? 0.0 : ac[r]) + em1;
-      }
-      tb.warp_reduce();
-      if (lane == 0) red[s * NW + warp] = tb;
-    }
-    worker_sync<WT>();
-
-    // Phase 2a: certified exact winner per segment (warps take segments in
-    // turn), sent to the head.
-    for (int s = warp; s < nseg; s += NW) {
-      const int j = ja + s;
-      int rb, re;
-      seg_of(s, rb, re);
-      Top2 tb;
-      tb.init();
-      if (lane < NW) tb = red[s * NW + lane];
-      tb.warp_reduce();
-      ExactBest eb;
-      eb.init();
-      if (tb.x1 != IDX_NONE) {
-        const int d1 = tb.x1;
-        int r1 = r0 - d1;
-        if (r1 < 0) r1 += D;
-        const int c1 = s * D + r1 - off0;
-        const unsigned short it = itil[c1];
-        const bool amb = (it & 0x8000) || ((tb.b1 - tb.b2) <= m.margin);
-        if (!amb) {
-          if (lane == 0) {
-            const int i1 = it & 0x7fff;
-            const double e = (t > D) ? acc_cur[c1] : early_window(m, B.ck, P.M, B.obs, t, d1, j);
-            eb.set((e + dsel[c1]) + (tr[s * N + i1] + dur[s * D + d1]), d1, i1);
-          }
-        } else {
-          // Re-score every candidate inside the margin exactly.
-          const long long thr = tb.b1 - m.margin;
-          bool ok = true;
-          for (int r = rb + lane; r < re; r += 32) {
-            int d = r0 - r;
-            if (d < 0) d += D;
-            if (d < L || d >= tau) continue;
-            const int c = s * D + r - off0;
-            if (ctil[c] + qd[s * D + d] < thr) continue;
-            const double e = (t > D) ? acc_cur[c] : early_window(m, B.ck, P.M, B.obs, t, d, j);
-            const double du = dur[s * D + d];
-            for (int i = 0; i < N && ok; ++i) {
-              double dv;
-              ok = load_dstar(B, P, N, t - 1 - d, i, dv);
-              if (ok) eb.offer((e + dv) + (tr[s * N + i] + du), d, i);
-            }
-          }
-          eb.warp_reduce();
-          if (!__all_sync(0xffffffffu, ok)) {
-            if (lane == 0) { grid_fail(B, TV_ETIMEOUT_DEV, SITE_WORKER_RESCORE); s_bad = 1; }
-          }
-        }
-      }
-      if (lane == 0) send_partial(B, P, (unsigned)t, prow, seg0 + s, eb);
-    }
-    // Phase 2b: intake of the slot that enters the worker domain at step t+1
-    // (s' = t-L, d = L then); the last warp, one lane per segment.  Lane 0
-    // waits for the slot message even when the slot is not its own: that is
-    // the flow control that keeps a worker at most L steps ahead of the head
-    // (its partials ring holds PART_RING steps).
-    if (warp == NW - 1 && lane < nseg && t + 1 < T && t - L >= 0) {
-      const long long sp = t - L;
-      int rn = r0 + 1 - L;
-      if (rn < 0) rn += D;
-      int rb, re;
-      seg_of(lane, rb, re);
-      const unsigned tag = (unsigned)(sp + 1);
-      const unsigned long long* msg =
-          B.slot_msg + ((size_t)((unsigned)sp & (SLOT_RING - 1)) * N + ja + lane) * SLOT_WORDS;
-      unsigned long long cbits, dbits, ibits;
-      if (rn < rb || rn >= re) {
-        if (lane == 0 && !tagged64_load(msg, tag, cbits, B.abort_flag, P.timeout)) {
-          grid_fail(B, TV_ETIMEOUT_DEV, SITE_WORKER_SLOT);
-          s_bad = 1;
-        }
-      } else {
-        bool ok = tagged64_load(msg, tag, cbits, B.abort_flag, P.timeout) &&
-                  tagged64_load(msg + 2, tag, dbits, B.abort_flag, P.timeout);
-        if (ok) {
-          unsigned long long iw = ld_relaxed_u64(msg + 4);
-          const long long t0 = clock64();
-          while ((unsigned)(iw >> 32) != tag) {
-            if (ld_relaxed_i32(B.abort_flag) || clock64() - t0 > P.timeout) { ok = false; break; }
-            iw = ld_relaxed_u64(msg + 4);
-          }
-          ibits = iw;
-        }
-        if (ok) {
-          const int c = lane * D + rn - off0;
-          ctil[c] = (long long)cbits;
-          dsel[c] = __longlong_as_double((long long)dbits);
-          itil[c] = (unsigned short)(ibits & 0xffff);
-        } else {
-          grid_fail(B, TV_ETIMEOUT_DEV, SITE_WORKER_SLOT);
-          s_bad = 1;
-        }
-      }
-    }
-    // Phase 2c: at t+1 = D+1 the first fold starts from the reference's
-    // newest-first sums of step D: E_{D+1}[d] = E_D[d-1] + em_{D+1}.
-    const bool seed = (t1 < T) && (t1 == D + 1);
-    if (seed) {
-      const int ot1 = B.obs[t1];
+      // Phase 1: fixed-point scan over d in [L, tau), fused with the exact
+      // window folds of step t+1 into the next buffer (src/hsmm.cu:298-310):
+      // E_{t+1}[d] = E_t[d-1] + em_{t+1}, E_{t+1}[0] = 0 + em_{t+1}.  The FP64
+      // adds overlap the integer scan.
+      const bool fold = (t1 < T) && (t1 > D + 1);
+      Top2* redb = red + (int)(t & 1) * P.max_seg * NW;
       for (int s = 0; s < nseg; ++s) {
         int rb, re;
         seg_of(s, rb, re);
-        const int j = ja + s;
-        const double em1 = m.em[(size_t)ot1 * N + j];
-        double* an = acc_nxt + s * D - off0;
+        const long long* ct = ctil + s * D - off0;
+        const long long* q = qd + s * D;
+        const double* ac = accb + a3 * accs + s * D - off0;
+        double* an = accb + an3 * accs + s * D - off0;
+        const double em1 = fold ? emw[(int)(t1 & 1) * P.max_seg + s] : 0.0;
+        Top2 tb;
+        tb.init();
+#pragma unroll 4
         for (int r = rb + tid; r < re; r += WT) {
-          int d = r0n - r;
+          int d = r0 - r;
           if (d < 0) d += D;
-          const double base = (d == 0) ? 0.0 : early_window(m, B.ck, P.M, B.obs, D, d - 1, j);
-          an[r] = base + em1;
+          if (d >= L && d < tau) tb.push(ct[r] + q[d], d);
+          if (fold) an[r] = ((r == r0n) ? 0.0 : ac[r]) + em1;
+        }
+        tb.warp_reduce();
+        if (lane == 0) redb[s * NW + warp] = tb;
+      }
+      // Phase 2c: at t+1 = D+1 the first fold starts from the reference's
+      // newest-first sums of step D: E_{D+1}[d] = E_D[d-1] + em_{D+1}.
+      if (t1 < T && t1 == D + 1) {
+        const int ot1 = B.obs[t1];
+        for (int s = 0; s < nseg; ++s) {
+          int rb, re;
+          seg_of(s, rb, re);
+          const int j = ja + s;
+          const double em1 = m.em[(size_t)ot1 * N + j];
+          double* an = accb + an3 * accs + s * D - off0;
+          for (int r = rb + tid; r < re; r += WT) {
+            int d = r0n - r;
+            if (d < 0) d += D;
+            const double base = (d == 0) ? 0.0 : early_window(m, B.ck, P.M, B.obs, D, d - 1, j);
+            an[r] = base + em1;
+          }
         }
       }
+      worker_sync_all<WT>();  // phase 1 of step t done; the service work of step t-1 done
+      if (*(volatile int*)&s_bad[(t - 1) & 1]) break;
+      r0 = r0n;
+      a3 = an3;
     }
-    worker_sync<WT>();
-    if (s_bad) return;
-    if (fold || seed) {
-      double* x = acc_cur;
-      acc_cur = acc_nxt;
-      acc_nxt = x;
+  } else {
+    for (long long t = 1; t < T; ++t) {
+      const int tau = (int)(t < D ? t : D);
+      int r0n = r0 + 1;
+      if (r0n == D) r0n = 0;
+      const int an3 = a3 == 2 ? 0 : a3 + 1;
+      worker_sync_all<WT>();
+      if (*(volatile int*)&s_bad[(t - 1) & 1]) break;
+      if (warp == NW) {
+        // Certify warp: the exact winner of each segment at step t, from the
+        // scan's best and runner-up; lanes in groups of NW, a group per
+        // segment, 32/NW segments at a time.
+        const Top2* redb = red + (int)(t & 1) * P.max_seg * NW;
+        const double* ac = accb + a3 * accs;  // E_t
+        const unsigned prow = (unsigned)t & (PART_RING - 1);
+        constexpr int GPW = 32 / NW;
+        const int grp = lane / NW, gi = lane % NW;
+        for (int s0 = 0; s0 < nseg; s0 += GPW) {
+          const int s = s0 + grp;
+          const bool sv = s < nseg;
+          Top2 tb;
+          tb.init();
+          if (sv) tb = redb[s * NW + gi];
+#pragma unroll
+          for (int o = NW / 2; o > 0; o >>= 1) {
+            const long long ob1 = __shfl_xor_sync(0xffffffffu, tb.b1, o);
+            const long long ob2 = __shfl_xor_sync(0xffffffffu, tb.b2, o);
+            const int ox1 = __shfl_xor_sync(0xffffffffu, tb.x1, o);
+            tb.merge(ob1, ox1, ob2);
+          }
+          ExactBest eb;
+          eb.init();
+          bool amb = false;
+          if (sv && gi == 0 && tb.x1 != IDX_NONE) {
+            const int d1 = tb.x1;
+            int r1 = r0 - d1;
+            if (r1 < 0) r1 += D;
+            const int c1 = s * D + r1 - off0;
+            const unsigned short it = itil[c1];
+            amb = (it & 0x8000) || ((tb.b1 - tb.b2) <= m.margin);
+            if (!amb) {
+              const int i1 = it & 0x7fff;
+              const double e = (t > D) ? ac[c1] : early_window(m, B.ck, P.M, B.obs, t, d1, ja + s);
+              eb.set((e + dsel[c1]) + (tr[s * N + i1] + dur[s * D + d1]), d1, i1);
+            }
+          }
+          // Ambiguous segments: the whole warp re-scores every candidate
+          // inside the margin exactly, one segment at a time.
+          unsigned am = __ballot_sync(0xffffffffu, amb);
+          while (am) {
+            const int src = __ffs(am) - 1;
+            am &= am - 1;
+            const int sa = s0 + src / NW;
+            const int j = ja + sa;
+            const long long thr = __shfl_sync(0xffffffffu, tb.b1, src) - m.margin;
+            int rb, re;
+            seg_of(sa, rb, re);
+            ExactBest ea;
+            ea.init();
+            bool ok = true;
+            for (int r = rb + lane; r < re; r += 32) {
+              int d = r0 - r;
+              if (d < 0) d += D;
+              if (d < L || d >= tau) continue;
+              const int c = sa * D + r - off0;
+              if (ctil[c] + qd[sa * D + d] < thr) continue;
+              const double e = (t > D) ? ac[c] : early_window(m, B.ck, P.M, B.obs, t, d, j);
+              const double du = dur[sa * D + d];
+              for (int i = 0; i < N && ok; ++i) {
+                double dv;
+                ok = load_dstar(B, P, N, t - 1 - d, i, dv);
+                if (ok) ea.offer((e + dv) + (tr[sa * N + i] + du), d, i);
+              }
+            }
+            ea.warp_reduce();
+            if (!__all_sync(0xffffffffu, ok)) {
+              if (lane == 0) {
+                grid_fail(B, TV_ETIMEOUT_DEV, SITE_WORKER_RESCORE);
+                s_bad[t & 1] = 1;
+              }
+            }
+            if (lane == src) eb = ea;
+          }
+          if (sv && gi == 0) send_partial(B, P, (unsigned)t, prow, seg0 + s, eb);
+        }
+      } else if (lane < nseg && t + 2 < T && t + 1 - L >= 0) {
+        // Intake warp, one lane per segment: the slot s' = t+1-L, which
+        // enters the scan at step t+2.  Lane 0 waits for the slot message
+        // even when the slot is not its own: that is the flow control that
+        // keeps a worker at most L-2 steps ahead of the head (its partials
+        // ring holds PART_RING steps).
+        const long long sp = t + 1 - L;
+        int rn = r0 + 2 - L;  // sp % D
+        if (rn < 0) rn += D;
+        int rb, re;
+        seg_of(lane, rb, re);
+        const unsigned tag = (unsigned)(sp + 1);
+        const unsigned long long* msg =
+            B.slot_msg + ((size_t)((unsigned)sp & (SLOT_RING - 1)) * N + ja + lane) * SLOT_WORDS;
+        const bool mine = rn >= rb && rn < re;
+        if (mine || lane == 0) {
+          unsigned long long cbits, dbits;
+          unsigned ibits;
+          if (!slot_load(msg, tag, cbits, dbits, ibits, B.abort_flag, P.timeout)) {
+            grid_fail(B, TV_ETIMEOUT_DEV, SITE_WORKER_SLOT);
+            s_bad[t & 1] = 1;
+          } else if (mine) {
+            const int c = lane * D + rn - off0;
+            ctil[c] = (long long)cbits;
+            dsel[c] = __longlong_as_double((long long)dbits);
+            itil[c] = (unsigned short)(ibits & 0xffff);
+          }
+        }
+      }
+      r0 = r0n;
+      a3 = an3;
     }
-    r0 = r0n;
   }
+  worker_sync_all<WT>();  // the service work of the last step is done
+  if (s_bad[0] | s_bad[1]) return;
+  if (!is_scan) return;
 
   // Tail at t = T-1: exhaustive exact scan of the worker's cells with the
   // survival function (src/hsmm.cu:101-137), one partial per segment.
@@ -479,6 +554,7 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
     const long long t = T - 1;
     const int tau = (int)(t < D ? t : D);
     const int rt = t >= 1 ? (int)((t - 1) % D) : 0;
+    const double* ac = accb + (size_t)(t % 3) * accs;  // E_{T-1}
     for (int s = 0; s < nseg; ++s) {
       int rb, re;
       seg_of(s, rb, re);
@@ -491,7 +567,7 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
         if (d < 0) d += D;
         if (d < L || d >= tau) continue;
         const int c = s * D + r - off0;
-        const double E = (t > D) ? acc_cur[c] : early_window(m, B.ck, P.M, B.obs, t, d, j);
+        const double E = (t > D) ? ac[c] : early_window(m, B.ck, P.M, B.obs, t, d, j);
         const double e = E + m.survT[(size_t)j * D + d];
         for (int i = 0; i < N && ok; ++i) {
           double dv;
@@ -501,10 +577,10 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
       }
       if (!ok) {
         grid_fail(B, TV_ETIMEOUT_DEV, SITE_WORKER_TAIL);
-        s_bad = 1;
+        s_bad[0] = 1;
       }
       eb = worker_reduce_exact<WT>(eb, ered);
-      if (s_bad) return;
+      if (s_bad[0]) return;
       if (tid == 0) send_partial(B, P, (unsigned)T, (unsigned)T & (PART_RING - 1), seg0 + s, eb);
     }
   }
@@ -544,7 +620,8 @@ constexpr int HWR = 4;  // rows of window sums kept by the head: steps t .. t+3
 // every thread is alive; threads without a role leave before the steps).
 // Non-aligned forms: they count threads, so a warp whose lanes took different
 // branches may arrive lane by lane.
-enum { BAR_STEP = 1, BAR_SLOT = 2, BAR_DENSE = 3, BAR_PW = 4 };
+enum { BAR_STEP = 1, BAR_SLOT0 = 2, BAR_DENSE = 3, BAR_PW0 = 4, BAR_SLOT1 = 5, BAR_PW1 = 6, BAR_PRE0 = 7,
+       BAR_PRE1 = 8, BAR_END = 9 };
 __device__ __forceinline__ void named_sync(int id, int count) {
   asm volatile("barrier.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
@@ -558,6 +635,40 @@ __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src)
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all_but_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// One-shot bulk copies (global -> shared) completed on an mbarrier: the
+// issuing thread announces the byte count, the copy engine moves the bytes
+// and completes the barrier's phase; a waiter polls the phase parity.
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  unsigned long long state;
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;" : "=l"(state) : "r"(a), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(d), "l"(src), "r"(bytes), "r"(a) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  unsigned ok;
+  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+               : "=r"(ok) : "r"(a), "r"(parity) : "memory");
+  return ok != 0;
+}
+// Waits (bounded) for the phase with the given parity to complete.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, long long limit) {
+  if (mbar_test(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_test(bar, parity))
+    if (clock64() - t0 > limit) return false;
+  return true;
+}
 
 __device__ __forceinline__ int coarse_of(long long fine_minus_base, int sh) {
   long long v = fine_minus_base >> sh;  // arithmetic shift: floor
@@ -630,32 +741,47 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   int* prei = (int*)(sm + P.h_prei);
   long long* prew = (long long*)(sm + P.h_prew);      // [2][N] best fixed-point score over d >= 1
   long long* preq = (long long*)(sm + P.h_preq);      // [2][N] fixed-point value of the exact winner
-  long long* pwq = (long long*)(sm + P.h_pwq);        // [S] worker partials of the next step
+  uint32_t* psirec = (uint32_t*)(sm + P.h_psirec);    // [2][N] back-pointer words, by step parity
+  long long* pwq = (long long*)(sm + P.h_pwq);        // [2][S] worker partials, by step parity
   long long* pwk = (long long*)(sm + P.h_pwk);
   int* pwd = (int*)(sm + P.h_pwd);
   int* pwi = (int*)(sm + P.h_pwi);
-  uint32_t* psirec = (uint32_t*)(sm + P.h_psirec);    // [2][N] back-pointer word of a step
   double* tail = (double*)(sm + P.h_tail);
+  // Failure flags: s_fail for the set-up and the tail; s_fb[t & 1] for an
+  // intake failure at step t of the loops (1), or the intake's notice that
+  // the loops end at step t-1 (2), read by every role at points where its
+  // value for step t is settled, so that all roles leave at the same step.
   __shared__ int s_fail;
+  __shared__ int s_fb[2];
+  __shared__ __align__(8) unsigned long long s_hwbar;  // completion of the window-sum row copies
   const int sh = P.coarse_shift;
   // Roles, by thread range:
-  //   [0, cs)             critical: the matvec, 4 lanes per state; the first
-  //                       cs_dense threads then run the dense phase, one lane per state
-  //   [cs, cs+st)         state helpers, one lane per state: step t+1's
-  //                       candidates, certification and exact winner, stores
-  //   [cs+st, cs+st+in)   intake of the workers' partial winners, one lane per
-  //                       segment; the first of these warps also computes the coarse base
+  //   [0, cs)               critical: the matvec, 4 (or 2) lanes per state; the
+  //                         first cs_dense threads then run the dense phase, one
+  //                         lane per state
+  //   [cs, cs+2*st)         state helpers in two groups, one lane per state;
+  //                         group g prepares step t+1 for the steps t of parity
+  //                         g (certification and exact winner over d >= 1), then
+  //                         stores step t-1's results; a group has two steps for
+  //                         its work, so its serial chain overlaps the other's
+  //   [cs+2*st, nthr)       intake: the workers' partial winners (a lane takes
+  //                         segments pk and pk + in), the emission prefix (one
+  //                         lane per state), the window-sum copies and the coarse
+  //                         base
   // Threads beyond these leave once the tables are set up.
   const int cs = P.cs_threads, st = P.st_threads, in = P.in_threads;
-  const int nthr = cs + st + in;
+  const int nthr = cs + 2 * st + in;
   const bool is_cs = tid < cs;
-  const bool is_st = !is_cs && tid < cs + st;
+  const bool is_st = !is_cs && tid < cs + 2 * st;
   const bool is_in = !is_cs && !is_st && tid < nthr;
   const int gj = tid / G4, gl = tid % G4;              // critical: state and lane of this group
-  const int sj = tid - cs;                             // state helper: state
-  const int pk = tid - cs - st;                        // intake: segment
+  const int sg = is_st ? (tid - cs) / st : 0;          // state helper: group (parity of its steps)
+  const int sj = is_st ? (tid - cs) % st : 0;          // state helper: state
+  const int pk = tid - cs - 2 * st;                    // intake: lane
   const bool has_sj = is_st && sj < N;
   const bool has_pk = is_in && pk < S;
+  const bool has_pk2 = is_in && pk + in < S;
+  const bool has_pj = is_in && pk < N;                 // in >= N: a lane per state too
   int k0 = 0, k1 = 0;
   if (has_sj) {
     k0 = B.seg_first[sj];
@@ -694,7 +820,12 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   }
   for (int k = tid; k < HWR * L * N; k += blockDim.x)  // window sums of steps 0..3
     if (k / (L * N) < T) hwr[k] = B.hwin[k];
-  if (tid == 0) s_fail = 0;
+  if (tid == 0) {
+    s_fail = 0;
+    s_fb[0] = 0;
+    s_fb[1] = 0;
+    mbar_init(&s_hwbar, 1);
+  }
   __syncthreads();
   if (warp == 0) {
     long long mx = LLONG_MIN;
@@ -705,31 +836,47 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   }
   __syncthreads();
   for (int jj = tid; jj < N; jj += blockDim.x) dqcp[jj] = coarse_of(dq[jj] - basebuf[0], sh) * 128;
-  // worker partials of step 1 (all empty: no d >= L yet), and the prefetch of step 2
-  TaggedMsg pm;
-  if (has_pk && T > 1) {
-    const unsigned long long* src = B.part + ((size_t)(1 & (PART_RING - 1)) * S + pk) * MSG_WORDS;
-    msg_load(src, pm);
-    if (!msg_wait(src, 1u, pm, B.abort_flag, P.timeout)) {
-      grid_fail(B, TV_ETIMEOUT_DEV, SITE_HEAD_PARTIAL);
-      s_fail = 1;
+  // worker partials of step 1 (all empty: no d >= L yet) into buffer 1, and
+  // the prefetch of step 2
+  TaggedMsg pm, pm2;
+  auto intake_one = [&](int seg, TaggedMsg& msg, long long step, int site, int* flag) {
+    const unsigned long long* src = B.part + ((size_t)((unsigned)step & (PART_RING - 1)) * S + seg) * MSG_WORDS;
+    if (!msg_wait(src, (unsigned)step, msg, B.abort_flag, P.timeout)) {
+      grid_fail(B, TV_ETIMEOUT_DEV, site);
+      *flag = 1;
     } else {
-      take_partial(pm, pk, P.qf, pwq, pwk, pwd, pwi);
+      const int pb = (int)(step & 1) * S;
+      take_partial(msg, seg, P.qf, pwq + pb, pwk + pb, pwd + pb, pwi + pb);
     }
-    if (T > 2) msg_load(B.part + ((size_t)(2 & (PART_RING - 1)) * S + pk) * MSG_WORDS, pm);
+  };
+  if (T > 1) {
+    if (has_pk) {
+      msg_load(B.part + ((size_t)(1 & (PART_RING - 1)) * S + pk) * MSG_WORDS, pm);
+      intake_one(pk, pm, 1, SITE_HEAD_PARTIAL, &s_fail);
+      if (T > 2) msg_load(B.part + ((size_t)(2 & (PART_RING - 1)) * S + pk) * MSG_WORDS, pm);
+    }
+    if (has_pk2) {
+      msg_load(B.part + ((size_t)(1 & (PART_RING - 1)) * S + pk + in) * MSG_WORDS, pm2);
+      intake_one(pk + in, pm2, 1, SITE_HEAD_PARTIAL, &s_fail);
+      if (T > 2) msg_load(B.part + ((size_t)(2 & (PART_RING - 1)) * S + pk + in) * MSG_WORDS, pm2);
+    }
   }
   __syncthreads();
   if (s_fail) return;
   for (int jj = tid; jj < N; jj += blockDim.x) {
     const int a = B.seg_first[jj], b = a + B.seg_count[jj];
     const long long p1 = ptil[N + jj];
+    const long long* pq1 = pwq + S;
+    const long long* pk1 = pwk + S;
+    const int* pd1 = pwd + S;
+    const int* pi1 = pwi + S;
     long long W = QNEG;
     for (int k = a; k < b; ++k)
-      if (pwd[k] != EMPTY_D) W = max(W, pwq[k] - p1);
+      if (pd1[k] != EMPTY_D) W = max(W, pq1[k] - p1);
     ExactBest eb;
     eb.init();
     for (int k = a; k < b; ++k)
-      if (pwd[k] != EMPTY_D && pwq[k] - p1 >= W - margin) eb.offer_key(pwk[k], pwd[k], pwi[k]);
+      if (pd1[k] != EMPTY_D && pq1[k] - p1 >= W - margin) eb.offer_key(pk1[k], pd1[k], pi1[k]);
     prew[(1 & 1) * N + jj] = W;
     prek[(1 & 1) * N + jj] = eb.k;
     pred[(1 & 1) * N + jj] = eb.d;
@@ -739,13 +886,14 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   __syncthreads();
   if (tid >= nthr) return;  // no role in the steps
 
-  // Register pipelines: a state helper keeps the prefix term of step t+2 and
-  // the observation of step t+3; an intake lane the partial message of step
-  // t+2 (in pm); a dense critical lane the initialisation score of step t+1.
+  // Register pipelines: an intake lane keeps the partial messages of step t+2
+  // (pm, pm2) and, for its state, the prefix term of step t+2 and the
+  // observation of step t+3; a dense critical lane the initialisation score of
+  // step t+1.
   long long qe_pf = 0;
   int ob_q = 0;
-  if (has_sj) {
-    if (2 < T) qe_pf = m.qem[(size_t)B.obs[2] * N + sj];
+  if (has_pj) {
+    if (2 < T) qe_pf = m.qem[(size_t)B.obs[2] * N + pk];
     if (3 < T) ob_q = B.obs[3];
   }
   double di_cur = 0.0;  // initialisation score of step t, state tid (dense critical lanes)
@@ -754,14 +902,43 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
 
   int drow_prev = 0;  // (t-1) % (L+1): row of delta[t-1] in dstar_h
   int rdrow = 1;      // t % Rd: row of delta[t] in the tagged ring
-  for (long long t = 1; t < T; ++t) {
-    const int cur = (int)(t & 1), prv = cur ^ 1;
-    const int drow = drow_prev + 1 == L + 1 ? 0 : drow_prev + 1;  // t % (L+1)
-    const int hrow = (int)((t - 1) & (L - 1));                      // slot t-1 in ctil_h
-    const long long t1 = t + 1;
-    const bool next = t1 < T;
-    const int nxt = cur ^ 1;  // (t+1) & 1
-    if (is_cs) {
+  // Service work of the critical warps' spare lanes at step t, while the
+  // dense phase runs (all inputs are complete: slot t-1 since the dense
+  // barrier, step t-1's results since the previous step): the slot t-1
+  // messages for the workers (score, selected delta[t-1][i*], argmax word),
+  // step t-1's back-pointers and delta[t-1] in the exact ring the workers
+  // read, and the coarse base of step t+1 (max_i delta[t-1], one warp).
+  auto cs_service = [&](int sx, int ns, long long t) {
+    const int hrow = (int)((t - 1) & (L - 1));
+    const int prv = (int)((t - 1) & 1);
+    const int rprev = rdrow == 0 ? P.Rd - 1 : rdrow - 1;  // (t-1) % Rd
+    const unsigned tag = (unsigned)t;
+    for (int j = sx; j < N; j += ns) {
+      const unsigned short itv = itil_h[hrow * N + j];
+      unsigned long long* msg = B.slot_msg + ((size_t)((unsigned)(t - 1) & (SLOT_RING - 1)) * N + j) * SLOT_WORDS;
+      tagged64_store(msg, tag, (unsigned long long)ctil_h[hrow * N + j]);
+      tagged64_store(msg + 2, tag, (unsigned long long)__double_as_longlong(dstar_h[drow_prev * N + (itv & 0x7fff)]));
+      st_relaxed_u64(msg + 4, ((unsigned long long)tag << 32) | itv);
+      if (t >= 2) {
+        B.psi[(size_t)(t - 1) * N + j] = psirec[prv * N + j];
+        tagged64_store(B.dstar + ((size_t)rprev * N + j) * 2, tag,
+                       (unsigned long long)__double_as_longlong(dstar_h[drow_prev * N + j]));
+      }
+    }
+    if (sx < 32) {
+      long long mx = LLONG_MIN;
+      for (int i = sx; i < N; i += 32) mx = max(mx, dq[prv * N + i]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      if (sx == 0) basebuf[(int)((t + 1) & 1)] = mx;
+    }
+  };
+  if (is_cs) {
+    // ================= critical warps: every step =================
+    for (long long t = 1; t < T; ++t) {
+      const int cur = (int)(t & 1), prv = cur ^ 1;
+      const int drow = drow_prev + 1 == L + 1 ? 0 : drow_prev + 1;  // t % (L+1)
+      const int hrow = (int)((t - 1) & (L - 1));                      // slot t-1 in ctil_h
       // ================= critical warps =================
       double di_next = 0.0;
       if (tid < N && t + 1 < D) di_next = __ldcg(B.dinit + (size_t)(t + 1) * N + tid);
@@ -816,9 +993,11 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
           itil_h[hrow * N + j] = (unsigned short)(ifine | (amb ? 0x8000 : 0));
         }
       }
-      named_arrive(BAR_SLOT, cs + st);  // slot t-1 ready for the state helpers
+      named_arrive(cur ? BAR_SLOT1 : BAR_SLOT0, cs + st);  // slot t-1 ready for the group of step t
+      named_sync(BAR_DENSE, cs);                            // every state's slot t-1 is in
       if (tid < P.cs_dense) {
-        named_sync(BAR_DENSE, cs);
+        // the winner over d >= 1 of step t, prepared by the group of step t-1
+        if (t >= 2) named_sync(prv ? BAR_PRE1 : BAR_PRE0, P.cs_dense + st);
         if (tid < N) {
           // dense phase, one lane per state; the exact d = 0 score of the
           // certified argmax over i is computed before it is known to be needed
@@ -834,7 +1013,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
           const double du0 = dur_h[dj * L];
           // src/hsmm.cu:341-346 with E_t[0]
           const double V0 = (e0 + dstar_h[drow_prev * N + i1]) + (trh[(size_t)dj * N + i1] + du0);
-          const long long q0 = quantize(V0, m.scale);
+          const long long q0 = fixed_from_double(V0, P.qf);
           long long kk = pk0, fq = pq0;
           int dd = pd0, ii = pi0;
           if (W0 >= Wt - margin) {
@@ -851,7 +1030,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
             kk = eb.k;
             dd = eb.d;
             ii = eb.i;
-            if (dd == 0) fq = (it & 0x8000) ? quantize(eb.value(), m.scale) : q0;
+            if (dd == 0) fq = (it & 0x8000) ? fixed_from_double(eb.value(), P.qf) : q0;
           }
           double fin = key_value(kk);
           uint32_t wv = pack_psi(dd, ii);
@@ -860,169 +1039,213 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
           if (t < D && !(kk > order_key(di_cur))) {
             fin = di_cur;
             wv = pack_psi((int)t, 0);
-            fq = quantize(fin, m.scale);
+            fq = fixed_from_double(fin, P.qf);
           }
           dstar_h[drow * N + dj] = fin;
           dq[cur * N + dj] = fq;
           dqcp[cur * Np + dj] = coarse_of(fq - basebuf[cur], sh) * 128;
           psirec[cur * N + dj] = wv;
         }
+        if (P.cs_dense == cs) cs_service(tid, cs, t);  // no spare warps: the dense lanes do it after
       } else {
-        named_arrive(BAR_DENSE, cs);
+        cs_service(tid - P.cs_dense, cs - P.cs_dense, t);
       }
       di_cur = di_next;
-    } else if (is_st) {
-      // ============ state helpers: prepare step t+1, one lane per state ============
-      // window sums of step t+3 into the ring; the copies of step t+2 are
-      // complete before this step's closing barrier
-      for (int c = sj; c < hw_chunks; c += st)
-        if (t + 3 < T)
-          cp_async16(hwr + (int)((t + 3) & (HWR - 1)) * L * N + c * 2, B.hwin + (size_t)(t + 3) * L * N + c * 2);
-      cp_async_commit();
-      cp_async_wait_all_but_1();
-      if (has_sj) {
-        if (next) {
-          ptil[(int)(t1 & 3) * N + sj] = ptil[(int)(t & 3) * N + sj] + qe_pf;  // P(t+1)
-          if (t + 2 < T) qe_pf = m.qem[(size_t)ob_q * N + sj];
-          if (t + 3 < T) ob_q = B.obs[t + 3];
-        }
-        // results of step t-1 to global memory
-        if (t >= 2) {
-          B.psi[(size_t)(t - 1) * N + sj] = psirec[prv * N + sj];
-          tagged64_store(B.dstar + ((size_t)(rdrow == 0 ? P.Rd - 1 : rdrow - 1) * N + sj) * 2, (unsigned)t,
-                         (unsigned long long)__double_as_longlong(dstar_h[drow_prev * N + sj]));
-        }
+      drow_prev = drow;
+      rdrow = rdrow + 1 == P.Rd ? 0 : rdrow + 1;
+      named_sync(BAR_STEP, cs + in);
+      if (*(volatile int*)&s_fb[cur]) break;  // the intake failed at this step
+    }
+  } else if (is_st) {
+    // ============ state helpers: group sg takes the steps of parity sg ============
+    for (long long t = sg ? 1 : 2; t < T; t += 2) {
+      const long long t1 = t + 1;
+      const bool next = t1 < T;
+      const int ti = (int)t;
+      const int bw = (int)(t1 & 1) * S;  // partial buffer of step t+1
+      named_sync(sg ? BAR_PW1 : BAR_PW0, st + in);  // partials of step t+1, P(t+1), window sums of t+1 are in
+      const int fb = *(volatile int*)&s_fb[sg];
+      if (fb == 2) break;  // the loops ended at step t-1
+      if (fb == 1) {       // the intake failed at this step: the critical warps finish it, then leave
+        named_sync(sg ? BAR_SLOT1 : BAR_SLOT0, cs + st);
+        break;
       }
-      named_sync(BAR_SLOT, cs + st);  // the critical warps published slot t-1
-      if (has_sj) {
-        // slot t-1 message for the workers
-        unsigned long long* msg =
-            B.slot_msg + ((size_t)((unsigned)(t - 1) & (SLOT_RING - 1)) * N + sj) * SLOT_WORDS;
-        const unsigned tag = (unsigned)t;
-        const unsigned short itv = itil_h[hrow * N + sj];
-        tagged64_store(msg, tag, (unsigned long long)ctil_h[hrow * N + sj]);
-        tagged64_store(msg + 2, tag,
-                       (unsigned long long)__double_as_longlong(dstar_h[drow_prev * N + (itv & 0x7fff)]));
-        st_relaxed_u64(msg + 4, ((unsigned long long)tag << 32) | itv);
-      }
-      named_sync(BAR_PW, st + in);  // the intake lanes took in the partials of step t+1
+      // Every candidate d >= 1 of step t+1 in fixed point: d = 1..L-1 here
+      // (slots t-d), d >= L as the workers' winners, whose fixed-point scores
+      // are their values minus the prefix P(t+1).  Only d = 1 needs slot t-1,
+      // which the critical warps are computing meanwhile: the rest (R) is
+      // certified first, with the exact winner among R within the margin of
+      // R's best, and the exact score of the best short candidate computed
+      // before it is known to be needed.
+      const int tau1 = (int)(t1 < D ? t1 : D);
+      const int hl1 = tau1 < L ? tau1 : L;
+      long long Wr = QNEG;
+      ExactBest er;
+      er.init();
+      long long qr = 0;
       if (has_sj && next) {
-        // Every candidate d >= 1 of step t+1 in fixed point: d = 1..L-1 here
-        // (slots t-d), d >= L as the workers' winners, whose fixed-point
-        // scores are their values minus the prefix P(t+1).  Written for
-        // instruction-level parallelism: one lane carries a state, so its
-        // loads are issued together and the exact score of the best short
-        // candidate is computed before it is known to be needed.
-        const int tau1 = (int)(t1 < D ? t1 : D);
-        const int hl1 = tau1 < L ? tau1 : L;
         const long long p1 = ptil[(int)(t1 & 3) * N + sj];
         long long Wd[L];
         unsigned short itd[L];
 #pragma unroll
-        for (int d = 1; d < L; ++d) {
-          const int row = (int)((t - d) & (L - 1));
+        for (int d = 2; d < L; ++d) {
+          const int row = (ti - d) & (L - 1);
           Wd[d] = d < hl1 ? ctil_h[row * N + sj] + qd_h[sj * L + d] : QNEG;
           itd[d] = itil_h[row * N + sj];
         }
-        long long Wh = QNEG;
+        long long Wh = QNEG, W2 = QNEG;
         int dh = 0, ih = 0, hamb = 0;
 #pragma unroll
-        for (int d = 1; d < L; ++d)
+        for (int d = 2; d < L; ++d) {
+          W2 = max(W2, min(Wh, Wd[d]));
           if (Wd[d] > Wh) {
             Wh = Wd[d];
             dh = d;
             ih = itd[d] & 0x7fff;
             hamb = itd[d] & 0x8000;
           }
+        }
         double Vh = 0.0;
         long long qh = 0;
         if (dh > 0) {
-          int dr = drow_prev + 1 - dh;  // row of delta[t-dh]
-          if (dr < 0) dr += L + 1;
+          const int dr = (ti - dh) % (L + 1);  // row of delta[t-dh]
           const double e = hwr[((int)(t1 & (HWR - 1)) * L + dh) * N + sj];
           Vh = (e + dstar_h[dr * N + ih]) + (trh[(size_t)sj * N + ih] + dur_h[sj * L + dh]);
-          qh = quantize(Vh, m.scale);
+          qh = fixed_from_double(Vh, P.qf);
         }
-        long long Wl = Wh;
+        Wr = Wh;
         for (int k = k0; k < k1; ++k)
-          if (pwd[k] != EMPTY_D) Wl = max(Wl, pwq[k] - p1);
-        const long long thr = Wl - margin;
-        // exact winner among the candidates within the margin of the best,
-        // with its fixed-point value
-        ExactBest eb;
-        eb.init();
-        long long qb = 0;
+          if (pwd[bw + k] != EMPTY_D) Wr = max(Wr, pwq[bw + k] - p1);
+        const long long thr = Wr - margin;
         for (int k = k0; k < k1; ++k)
-          if (pwd[k] != EMPTY_D && pwq[k] - p1 >= thr && eb.better_key(pwk[k], pwd[k], pwi[k])) {
-            eb.k = pwk[k];
-            eb.d = pwd[k];
-            eb.i = pwi[k];
-            qb = pwq[k];
+          if (pwd[bw + k] != EMPTY_D && pwq[bw + k] - p1 >= thr &&
+              er.better_key(pwk[bw + k], pwd[bw + k], pwi[bw + k])) {
+            er.k = pwk[bw + k];
+            er.d = pwd[bw + k];
+            er.i = pwi[bw + k];
+            qr = pwq[bw + k];
           }
-        int nh = 0;
-#pragma unroll
-        for (int d = 1; d < L; ++d) nh += Wd[d] >= thr ? 1 : 0;
-        if (nh == 1 && !hamb) {
-          const long long kh = order_key(Vh);
-          if (eb.better_key(kh, dh, ih)) {
-            eb.k = kh;
-            eb.d = dh;
-            eb.i = ih;
-            qb = qh;
-          }
-        } else if (nh > 0) {
-          // several short candidates in the margin, or an ambiguous argmax over i
-          for (int d = 1; d < hl1; ++d) {
-            if (Wd[d] < thr) continue;
-            const double e = hwr[((int)(t1 & (HWR - 1)) * L + d) * N + sj];
-            const double du = dur_h[sj * L + d];
-            int dr = drow_prev + 1 - d;  // row of delta[t-d]
-            if (dr < 0) dr += L + 1;
-            const double* drw = dstar_h + dr * N;
-            const double* trj = trh + (size_t)sj * N;
-            const unsigned short it = itd[d];
-            if (!(it & 0x8000)) {
-              const int i1 = it & 0x7fff;
-              eb.offer((e + drw[i1]) + (trj[i1] + du), d, i1);
-            } else {
-              for (int i = 0; i < N; ++i) eb.offer((e + drw[i]) + (trj[i] + du), d, i);
+        if (Wh >= thr) {
+          if (W2 < thr && !hamb) {
+            // one short candidate in the margin, argmax over i certified
+            const long long kh = order_key(Vh);
+            if (er.better_key(kh, dh, ih)) {
+              er.k = kh;
+              er.d = dh;
+              er.i = ih;
+              qr = qh;
             }
+          } else {
+            // several in the margin, or an ambiguous argmax over i (rare)
+            for (int d = 2; d < hl1; ++d) {
+              if (Wd[d] < thr) continue;
+              const double e = hwr[((int)(t1 & (HWR - 1)) * L + d) * N + sj];
+              const double du = dur_h[sj * L + d];
+              const double* drw = dstar_h + ((ti - d) % (L + 1)) * N;
+              const double* trj = trh + (size_t)sj * N;
+              const unsigned short it = itd[d];
+              if (!(it & 0x8000)) {
+                const int i1 = it & 0x7fff;
+                er.offer((e + drw[i1]) + (trj[i1] + du), d, i1);
+              } else {
+                for (int i = 0; i < N; ++i) er.offer((e + drw[i]) + (trj[i] + du), d, i);
+              }
+            }
+            qr = er.d == IDX_NONE ? 0 : fixed_from_double(er.value(), P.qf);
           }
-          qb = eb.d == IDX_NONE ? 0 : quantize(eb.value(), m.scale);
         }
-        prew[nxt * N + sj] = Wl;
-        prek[nxt * N + sj] = eb.k;
-        pred[nxt * N + sj] = eb.d;
-        prei[nxt * N + sj] = eb.i;
-        preq[nxt * N + sj] = qb;
       }
-    } else {
-      // ============ intake: worker partials of step t+1, loaded during the previous step ============
-      if (has_pk && next) {
-        if (!msg_wait(B.part + ((size_t)((unsigned)t1 & (PART_RING - 1)) * S + pk) * MSG_WORDS, (unsigned)t1, pm,
-                      B.abort_flag, P.timeout)) {
-          grid_fail(B, TV_ETIMEOUT_DEV, SITE_HEAD_PARTIAL);
-          s_fail = 1;
+      named_sync(sg ? BAR_SLOT1 : BAR_SLOT0, cs + st);  // the critical warps published slot t-1
+      const int hrow = (ti - 1) & (L - 1);               // slot t-1
+      const int drw1 = (ti - 1) % (L + 1);               // row of delta[t-1]
+      if (has_sj && next) {
+        // d = 1 (slot t-1): merged exactly when it is within the margin of R
+        const long long W1 = hl1 > 1 ? ctil_h[hrow * N + sj] + qd_h[sj * L + 1] : QNEG;
+        const unsigned short it1 = itil_h[hrow * N + sj];
+        if (hl1 > 1 && W1 >= Wr - margin) {
+          const double e = hwr[((int)(t1 & (HWR - 1)) * L + 1) * N + sj];
+          const double du = dur_h[sj * L + 1];
+          const double* drw = dstar_h + drw1 * N;
+          const double* trj = trh + (size_t)sj * N;
+          if (!(it1 & 0x8000)) {
+            const int i1 = it1 & 0x7fff;
+            const double V1 = (e + drw[i1]) + (trj[i1] + du);
+            const long long k1v = order_key(V1);
+            if (er.better_key(k1v, 1, i1)) {
+              er.k = k1v;
+              er.d = 1;
+              er.i = i1;
+              qr = fixed_from_double(V1, P.qf);
+            }
+          } else {
+            for (int i = 0; i < N; ++i) er.offer((e + drw[i]) + (trj[i] + du), 1, i);
+            qr = er.d == IDX_NONE ? 0 : fixed_from_double(er.value(), P.qf);
+          }
+        }
+        const int nx = (int)(t1 & 1);
+        prew[nx * N + sj] = max(Wr, W1);
+        prek[nx * N + sj] = er.k;
+        pred[nx * N + sj] = er.d;
+        prei[nx * N + sj] = er.i;
+        preq[nx * N + sj] = qr;
+      }
+      if (next) named_arrive(sg ? BAR_PRE1 : BAR_PRE0, P.cs_dense + st);
+    }
+  } else {
+    // ============ intake: every step ============
+    long long last_copy = -1;  // a window-sum copy issued and not yet waited for
+    for (long long t = 1; t < T; ++t) {
+      const long long t1 = t + 1;
+      const bool next = t1 < T;
+      const int cur = (int)(t & 1), prv = cur ^ 1;
+      // worker partials of step t+1 (loaded during the previous step) into buffer (t+1) & 1
+      if (next) {
+        if (has_pk) {
+          intake_one(pk, pm, t1, SITE_HEAD_PARTIAL, &s_fb[cur]);
+          if (t1 + 1 < T) msg_load(B.part + ((size_t)((unsigned)(t1 + 1) & (PART_RING - 1)) * S + pk) * MSG_WORDS, pm);
+        }
+        if (has_pk2) {
+          intake_one(pk + in, pm2, t1, SITE_HEAD_PARTIAL, &s_fb[cur]);
+          if (t1 + 1 < T)
+            msg_load(B.part + ((size_t)((unsigned)(t1 + 1) & (PART_RING - 1)) * S + pk + in) * MSG_WORDS, pm2);
+        }
+        if (has_pj) {
+          ptil[(int)(t1 & 3) * N + pk] = ptil[(int)(t & 3) * N + pk] + qe_pf;  // P(t+1)
+          if (t + 2 < T) qe_pf = m.qem[(size_t)ob_q * N + pk];
+          if (t + 3 < T) ob_q = B.obs[t + 3];
+        }
+      }
+      // the window sums of step t+2 (copied during the previous step) are in
+      // before the group of step t+1 is released
+      if (pk == 0 && t >= 2 && t + 2 < T) {
+        if (mbar_wait(&s_hwbar, (unsigned)(t & 1), P.timeout)) {
+          last_copy = -1;
         } else {
-          take_partial(pm, pk, P.qf, pwq, pwk, pwd, pwi);
+          grid_fail(B, TV_ETIMEOUT_DEV, SITE_HEAD_COPY);
+          s_fb[cur] = 1;
         }
-        if (t1 + 1 < T) msg_load(B.part + ((size_t)((unsigned)(t1 + 1) & (PART_RING - 1)) * S + pk) * MSG_WORDS, pm);
       }
-      named_arrive(BAR_PW, st + in);
-      // coarse base of step t+1: max_i delta[t-1] (the first intake warp)
-      if (pk < 32) {
-        long long mx = LLONG_MIN;
-        for (int i = pk; i < N; i += 32) mx = max(mx, dq[prv * N + i]);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (pk == 0) basebuf[nxt] = mx;
+      named_arrive(cur ? BAR_PW1 : BAR_PW0, st + in);
+      // window sums of step t+3 into the ring: one bulk copy
+      if (pk == 0 && t + 3 < T) {
+        bulk_copy_g2s(hwr + (int)((t + 3) & (HWR - 1)) * L * N, B.hwin + (size_t)(t + 3) * L * N,
+                      (unsigned)(L * N * sizeof(double)), &s_hwbar);
+        last_copy = t - 1;  // the copy's index: it completes the barrier's phase t-1
+      }
+      named_sync(BAR_STEP, cs + in);
+      if (*(volatile int*)&s_fb[cur]) {
+        // the intake failed at this step: the group of step t+1 waits for its
+        // partials; wake it with the notice that the loops end here
+        s_fb[prv] = 2;
+        named_arrive(prv ? BAR_PW1 : BAR_PW0, st + in);
+        break;
       }
     }
-    drow_prev = drow;
-    rdrow = rdrow + 1 == P.Rd ? 0 : rdrow + 1;
-    named_sync(BAR_STEP, nthr);
-    if (s_fail) return;
+    // a copy still in flight after an early exit
+    if (pk == 0 && last_copy >= 0 && !mbar_wait(&s_hwbar, (unsigned)(last_copy & 1), P.timeout)) s_fb[0] = 1;
   }
+  named_sync(BAR_END, nthr);
+  if (s_fb[0] | s_fb[1]) return;
 
   // Tail at t = T-1 (src/hsmm.cu:101-137).
   {
@@ -1030,16 +1253,14 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
     const int tau = (int)(t < D ? t : D);
     const int hl = tau < L ? tau : L;
     if (has_pk) {
-      const unsigned long long* src = B.part + ((size_t)((unsigned)T & (PART_RING - 1)) * S + pk) * MSG_WORDS;
-      msg_load(src, pm);
-      if (!msg_wait(src, (unsigned)T, pm, B.abort_flag, P.timeout)) {
-        grid_fail(B, TV_ETIMEOUT_DEV, SITE_HEAD_TAIL);
-        s_fail = 1;
-      } else {
-        take_partial(pm, pk, P.qf, pwq, pwk, pwd, pwi);
-      }
+      msg_load(B.part + ((size_t)((unsigned)T & (PART_RING - 1)) * S + pk) * MSG_WORDS, pm);
+      intake_one(pk, pm, T, SITE_HEAD_TAIL, &s_fail);
     }
-    named_sync(BAR_STEP, nthr);
+    if (has_pk2) {
+      msg_load(B.part + ((size_t)((unsigned)T & (PART_RING - 1)) * S + pk + in) * MSG_WORDS, pm2);
+      intake_one(pk + in, pm2, T, SITE_HEAD_TAIL, &s_fail);
+    }
+    named_sync(BAR_END, nthr);
     if (s_fail) return;
     if (is_cs && gj < N) {
       const int j = gj;
@@ -1047,10 +1268,8 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
       eb.init();
       for (int d = gl; d < hl; d += G4) {
         const double e = hwr[((int)(t & (HWR - 1)) * L + d) * N + j] + m.survT[(size_t)j * D + d];
-        // after the loop drow_prev is the row of delta[T-1]; the tail reads
-        // delta[t-1-d] = delta[T-2-d]
-        int dr = drow_prev - 1 - d;
-        while (dr < 0) dr += L + 1;
+        // the tail reads delta[t-1-d] = delta[T-2-d]
+        const int dr = (int)((T - 2 - d) % (L + 1));
         const double* row = dstar_h + dr * N;
         const double* trj = trh + (size_t)j * N;
         for (int i = 0; i < N; ++i) eb.offer((e + row[i]) + trj[i], d, i);
@@ -1058,14 +1277,15 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
       group_reduce_exact<G4>(eb, gmask);
       if (gl == 0) {
         const int a = B.seg_first[j], b = a + B.seg_count[j];
+        const int tb_ = (int)(T & 1) * S;  // the tail partials' buffer
         for (int k = a; k < b; ++k)
-          if (pwd[k] != EMPTY_D) eb.offer_key(pwk[k], pwd[k], pwi[k]);
+          if (pwd[tb_ + k] != EMPTY_D) eb.offer_key(pwk[tb_ + k], pwd[tb_ + k], pwi[tb_ + k]);
         if (eb.d == IDX_NONE) { eb.d = 0; eb.i = 0; }
         tail[j] = eb.value();
         B.psi[(size_t)t * N + j] = pack_psi(eb.d, eb.i);
       }
     }
-    named_sync(BAR_STEP, nthr);
+    named_sync(BAR_END, nthr);
   }
 
   // Backtrace (src/hsmm.cu:139-170).
@@ -1100,7 +1320,7 @@ __global__ void __launch_bounds__(GRID_THREADS, 1) grid_decode_kernel(ModelView 
   if (ld_relaxed_i32(B.abort_flag)) return;  // rejected observations
   if (blockIdx.x == 0) {
     grid_head<G4>(m, P, B, smem);
-  } else if (threadIdx.x < (GW ? WORKER_THREADS_GW : WORKER_THREADS)) {
+  } else if (threadIdx.x < (GW ? WORKER_THREADS_GW : WORKER_THREADS) + WORKER_SERVICE) {
     grid_worker<GW>(m, P, B, smem);
   }
 }

@@ -387,27 +387,33 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
       max_seg = std::max(max_seg, jb - ja + 1);
     }
   };
-  // Head roles: 4 matvec lanes per state when everything fits the block, else 2.
-  auto head_roles_fit = [&](int S_) {
-    const int st = (N + 31) / 32 * 32, in = (S_ + 31) / 32 * 32;
-    return (2 * N + 31) / 32 * 32 + st + in <= tv::GRID_THREADS;
-  };
+  // Head roles: the critical warps (4 matvec lanes per state when everything
+  // fits the block, else 2), two state-helper groups of a lane per state, and
+  // intake lanes that take two segments each and cover the states.
+  auto round32 = [](int x) { return (x + 31) / 32 * 32; };
+  auto intake_threads = [&](int S_) { return round32(std::max((S_ + 1) / 2, N)); };
+  auto head_threads = [&](int g4, int S_) { return round32(g4 * N) + 2 * round32(N) + intake_threads(S_); };
+  auto head_roles_fit = [&](int S_) { return head_threads(2, S_) <= tv::GRID_THREADS; };
   // Cells are split per state (row-aligned) when every state gets whole
   // workers, so that a worker's duration and transition rows are one state's;
   // otherwise in equal contiguous chunks that may span states.
   partition(true);
   // Window in shared memory when a worker's share fits there: the duration
   // rows (8 B fixed point + 8 B exact per d) and transition rows of its
-  // states, and per cell the slot score, selected delta, two window-sum
-  // buffers (8 B each) and the argmax word (2 B).
+  // states, and per cell the slot score, selected delta, three window-sum
+  // buffers (8 B each) and the argmax word (2 B); the scan's per-warp
+  // results for two steps.
+  auto red_bytes = [&](int nw) {
+    return (unsigned long long)std::max(2 * max_seg * nw * sizeof(tv::Top2), 32 * sizeof(tv::ExactBest));
+  };
   auto smem_window_bytes = [&]() {
     unsigned long long o = 0;
     o = tv::tv_align(o + (unsigned long long)max_seg * D * 8);
     o = tv::tv_align(o + (unsigned long long)max_seg * D * 8);
     o = tv::tv_align(o + (unsigned long long)max_seg * N * 8);
-    for (int a = 0; a < 4; ++a) o = tv::tv_align(o + (unsigned long long)chunk * 8);
+    for (int a = 0; a < 5; ++a) o = tv::tv_align(o + (unsigned long long)chunk * 8);
     o = tv::tv_align(o + (unsigned long long)chunk * 2);
-    o = tv::tv_align(o + (unsigned long long)std::max(max_seg * (tv::WORKER_THREADS / 32) * sizeof(tv::Top2), 32 * sizeof(tv::ExactBest)));
+    o = tv::tv_align(o + red_bytes(tv::WORKER_THREADS / 32));
     o = tv::tv_align(o + (unsigned long long)2 * max_seg * 8);
     return o;
   };
@@ -437,10 +443,10 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
     P.w_tr = o;   o = tv::tv_align(o + (unsigned long long)max_seg * N * 8);
     P.w_ctil = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
     P.w_dsel = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
-    P.w_acc0 = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
-    P.w_acc1 = o; o = tv::tv_align(o + (unsigned long long)chunk * 8);
+    P.w_accs = tv::tv_align((unsigned long long)chunk * 8);
+    P.w_acc = o;  o += 3 * P.w_accs;
     P.w_itil = o; o = tv::tv_align(o + (unsigned long long)chunk * 2);
-    P.w_red = o;  o = tv::tv_align(o + (unsigned long long)std::max(max_seg * (tv::WORKER_THREADS / 32) * sizeof(tv::Top2), 32 * sizeof(tv::ExactBest)));
+    P.w_red = o;  o = tv::tv_align(o + red_bytes(tv::WORKER_THREADS / 32));
     P.w_emw = o;  o = tv::tv_align(o + (unsigned long long)2 * max_seg * 8);
     P.w_bytes = o;
   } else {
@@ -450,12 +456,12 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
     unsigned long long g = 0;
     P.w_ctil = g; g = tv::tv_align(g + (unsigned long long)chunk * 8);
     P.w_dsel = g; g = tv::tv_align(g + (unsigned long long)chunk * 8);
-    P.w_acc0 = g; g = tv::tv_align(g + (unsigned long long)chunk * 8);
-    P.w_acc1 = g; g = tv::tv_align(g + (unsigned long long)chunk * 8);
+    P.w_accs = tv::tv_align((unsigned long long)chunk * 8);
+    P.w_acc = g;  g += 3 * P.w_accs;
     P.w_itil = g; g = tv::tv_align(g + (unsigned long long)chunk * 2);
     P.w_gstride = (g + 255) / 256 * 256;
     P.w_qd = P.w_dur = P.w_tr = 0;
-    P.w_red = o;  o = tv::tv_align(o + (unsigned long long)std::max(max_seg * (tv::WORKER_THREADS_GW / 32) * sizeof(tv::Top2), 32 * sizeof(tv::ExactBest)));
+    P.w_red = o;  o = tv::tv_align(o + red_bytes(tv::WORKER_THREADS_GW / 32));
     P.w_emw = o;  o = tv::tv_align(o + (unsigned long long)2 * max_seg * 8);
     P.w_bytes = o;
   }
@@ -463,16 +469,13 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
   const int Np = (N + 15) / 16 * 16;
   P.Np = Np;
   // 4 matvec lanes per state when the roles fit the block, else 2
-  P.head_group = tv::HEAD_GROUP;
-  P.cs_threads = (P.head_group * N + 31) / 32 * 32;
-  if (P.cs_threads + (N + 31) / 32 * 32 + (S + 31) / 32 * 32 > tv::GRID_THREADS) {
-    P.head_group = 2;
-    P.cs_threads = (P.head_group * N + 31) / 32 * 32;
-  }
-  P.cs_dense = (N + 31) / 32 * 32;
-  P.st_threads = (N + 31) / 32 * 32;
-  P.in_threads = (S + 31) / 32 * 32;
-  P.block = std::max(P.cs_threads + P.st_threads + P.in_threads, P.w_global ? tv::WORKER_THREADS_GW : tv::WORKER_THREADS);
+  P.head_group = head_threads(tv::HEAD_GROUP, S) <= tv::GRID_THREADS ? tv::HEAD_GROUP : 2;
+  P.cs_threads = round32(P.head_group * N);
+  P.cs_dense = round32(N);
+  P.st_threads = round32(N);
+  P.in_threads = intake_threads(S);
+  P.block = std::max(P.cs_threads + 2 * P.st_threads + P.in_threads,
+                     (P.w_global ? tv::WORKER_THREADS_GW : tv::WORKER_THREADS) + tv::WORKER_SERVICE);
   if (P.block > tv::GRID_THREADS) return false;
   P.h_qcp = o;    o = tv::tv_align(o + (unsigned long long)N * Np * 4);
   P.h_dqcp = o;   o = tv::tv_align(o + (unsigned long long)2 * Np * 4);
@@ -490,10 +493,10 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
   P.h_prei = o;   o = tv::tv_align(o + (unsigned long long)2 * N * 4);
   P.h_prew = o;   o = tv::tv_align(o + (unsigned long long)2 * N * 8);
   P.h_preq = o;   o = tv::tv_align(o + (unsigned long long)2 * N * 8);
-  P.h_pwq = o;    o = tv::tv_align(o + (unsigned long long)S * 8);
-  P.h_pwk = o;    o = tv::tv_align(o + (unsigned long long)S * 8);
-  P.h_pwd = o;    o = tv::tv_align(o + (unsigned long long)S * 4);
-  P.h_pwi = o;    o = tv::tv_align(o + (unsigned long long)S * 4);
+  P.h_pwq = o;    o = tv::tv_align(o + (unsigned long long)2 * S * 8);
+  P.h_pwk = o;    o = tv::tv_align(o + (unsigned long long)2 * S * 8);
+  P.h_pwd = o;    o = tv::tv_align(o + (unsigned long long)2 * S * 4);
+  P.h_pwi = o;    o = tv::tv_align(o + (unsigned long long)2 * S * 4);
   P.h_psirec = o; o = tv::tv_align(o + (unsigned long long)2 * N * 4);
   P.h_tail = o;   o = tv::tv_align(o + (unsigned long long)N * 8);
   // The exact transition matrix and its fixed-point copy join the head's
@@ -669,8 +672,8 @@ int read_grid_status(tv_model_s* m, cudaStream_t st) {
   if (s[2] == tv::TV_ETIMEOUT_DEV) {
     static const char* sites[] = {"?", "head waiting for worker partials", "worker waiting for a slot message",
                                   "worker re-scoring waiting for an exact score", "worker tail waiting for an exact score",
-                                  "head waiting for tail partials"};
-    const int k = (s[0] >= 1 && s[0] <= 5) ? s[0] : 0;
+                                  "head waiting for tail partials", "head waiting for a window-sum copy"};
+    const int k = (s[0] >= 1 && s[0] <= 6) ? s[0] : 0;
     return fail(TV_ETIMEOUT, std::string("grid decode: a bounded wait between CTAs timed out (") + sites[k] + ")");
   }
   if (s[2] == TV_ERANGE) return fail(TV_ERANGE, "an observation is outside [0, O)");
