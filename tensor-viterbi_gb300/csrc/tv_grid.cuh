@@ -48,7 +48,6 @@ constexpr int CK_STRIDE = 32;      // checkpoint stride of the early window sums
 constexpr int PART_RING = 32;      // steps of worker partials in flight
 constexpr int SLOT_RING = 64;      // slot messages kept
 constexpr int SLOT_WORDS = 5;      // ctil (2), dsel (2), itil (1)
-constexpr int HEAD_GROUP = 4;      // lanes per state in the head's matvec (2 when N is too large for 4)
 constexpr int GRID_MAX_N = 128;    // packed coarse scores keep the state index in 7 bits
 constexpr int COARSE_F = 14;       // fraction bits of the packed coarse matvec scores
 constexpr int COARSE_CLAMP = (1 << 23) - 1;
@@ -67,14 +66,12 @@ struct GridParams {
       h_prek, h_pred, h_prei, h_prew, h_preq, h_pwq, h_pwk, h_pwd, h_pwi, h_psirec, h_tail, h_bytes;
   int trans_smem;     // the exact transition matrix is kept in the head's shared memory
   int qtr_smem;       // so is its fixed-point copy (else computed from the exact one)
-  int cs_dense;       // critical threads of the dense (one lane per state) phase: N rounded up to 32
   int st_threads;     // state helper threads per group (two groups): N rounded up to 32
   int in_threads;     // intake threads: max(ceil(S/2), N) rounded up to 32
   int block;          // threads per CTA: the head's roles (at least a worker's scan and service threads)
-  int head_group;     // matvec lanes per state in the head (4, or 2 for large N)
   int qf;             // fraction bits of the fixed-point scores
   int Np;             // N rounded up to 16 (packed coarse matvec rows)
-  int cs_threads;     // critical-section threads (4 lanes per state, whole warps)
+  int cs_threads;     // critical threads: one lane per state, N rounded up to 32
   int coarse_shift;   // fine-to-coarse right shift (f - COARSE_F)
   int coarse_margin;  // certified coarse i-margin, coarse units
   long long timeout;
@@ -276,7 +273,9 @@ __device__ __forceinline__ void send_partial(const GridBufs& B, const GridParams
                                              int seg, const ExactBest& eb) {
   TaggedMsg msg;
   const bool empty = eb.d == IDX_NONE;
-  msg_pack(msg, tag, eb.value(), empty ? EMPTY_D : eb.d, empty ? 0 : eb.i);
+  // the winner's order key and fixed-point value, and (d, i)
+  msg_pack(msg, tag, eb.k, empty ? 0 : fixed_from_double(eb.value(), P.qf),
+           empty ? ((unsigned)EMPTY_D << 16) : (((unsigned)eb.d << 16) | (unsigned)eb.i));
   msg_store(B.part + ((size_t)ring * P.S + seg) * MSG_WORDS, msg);
 }
 
@@ -620,8 +619,8 @@ constexpr int HWR = 4;  // rows of window sums kept by the head: steps t .. t+3
 // every thread is alive; threads without a role leave before the steps).
 // Non-aligned forms: they count threads, so a warp whose lanes took different
 // branches may arrive lane by lane.
-enum { BAR_STEP = 1, BAR_SLOT0 = 2, BAR_DENSE = 3, BAR_PW0 = 4, BAR_SLOT1 = 5, BAR_PW1 = 6, BAR_PRE0 = 7,
-       BAR_PRE1 = 8, BAR_END = 9 };
+enum { BAR_STEP = 1, BAR_SLOT0 = 2, BAR_PW0 = 4, BAR_SLOT1 = 5, BAR_PW1 = 6, BAR_PRE0 = 7, BAR_PRE1 = 8,
+       BAR_END = 9 };
 __device__ __forceinline__ void named_sync(int id, int count) {
   asm volatile("barrier.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
@@ -648,9 +647,8 @@ __device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned coun
 __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
   const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
-  unsigned long long state;
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;" : "=l"(state) : "r"(a), "r"(bytes) : "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                ::"r"(d), "l"(src), "r"(bytes), "r"(a) : "memory");
 }
@@ -683,36 +681,25 @@ __device__ __forceinline__ void packed_push(int p, int& b1, int& b2) {
   b2 = max(b2, lo);
 }
 
-template <int G4>
-__device__ __forceinline__ void group_reduce_exact(ExactBest& eb, unsigned gmask) {
-#pragma unroll
-  for (int o = G4 / 2; o > 0; o >>= 1) {
-    const long long ok = __shfl_xor_sync(gmask, eb.k, o);
-    const int od = __shfl_xor_sync(gmask, eb.d, o);
-    const int oi = __shfl_xor_sync(gmask, eb.i, o);
-    eb.offer_key(ok, od, oi);
-  }
-}
 
 // A worker segment's exact winner, kept as its order key and its fixed-point
-// value (the value of the segment's best candidate, to within half a unit).
-__device__ __forceinline__ void take_partial(const TaggedMsg& pm, int k, int qf, long long* pwq, long long* pwk,
-                                             int* pwd, int* pwi) {
-  double v;
-  int d, i;
-  msg_unpack(pm, v, d, i);
-  pwq[k] = d != EMPTY_D ? fixed_from_double(v, qf) : 0;
-  pwk[k] = order_key(v);
-  pwd[k] = d;
-  pwi[k] = i;
+// value (the value of the segment's best candidate, to within half a unit),
+// both computed by the worker.
+__device__ __forceinline__ void take_partial(const TaggedMsg& pm, int k, long long* pwq, long long* pwk, int* pwd,
+                                             int* pwi) {
+  long long key, fx;
+  unsigned di;
+  msg_unpack(pm, key, fx, di);
+  pwq[k] = fx;
+  pwk[k] = key;
+  pwd[k] = (int)(di >> 16);
+  pwi[k] = (int)(di & 0xffff);
 }
 
-template <int G4>
 __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBufs& B, unsigned char* sm) {
   constexpr int L = GRID_L;
   const int N = m.N, D = m.D, S = P.S, Np = P.Np;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const unsigned gmask = ((1u << G4) - 1) << ((lane / G4) * G4);
   const long long T = B.T;
   const long long margin = m.margin;
   int* Qcp = (int*)(sm + P.h_qcp);                    // [N][Np] packed coarse trans
@@ -741,7 +728,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   int* prei = (int*)(sm + P.h_prei);
   long long* prew = (long long*)(sm + P.h_prew);      // [2][N] best fixed-point score over d >= 1
   long long* preq = (long long*)(sm + P.h_preq);      // [2][N] fixed-point value of the exact winner
-  uint32_t* psirec = (uint32_t*)(sm + P.h_psirec);    // [2][N] back-pointer words, by step parity
+  uint32_t* psirec = (uint32_t*)(sm + P.h_psirec);    // [4][N] back-pointer words, row t % 4
   long long* pwq = (long long*)(sm + P.h_pwq);        // [2][S] worker partials, by step parity
   long long* pwk = (long long*)(sm + P.h_pwk);
   int* pwd = (int*)(sm + P.h_pwd);
@@ -756,14 +743,14 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   __shared__ __align__(8) unsigned long long s_hwbar;  // completion of the window-sum row copies
   const int sh = P.coarse_shift;
   // Roles, by thread range:
-  //   [0, cs)               critical: the matvec, 4 (or 2) lanes per state; the
-  //                         first cs_dense threads then run the dense phase, one
-  //                         lane per state
+  //   [0, cs)               critical: one lane per state, the matvec of slot
+  //                         t-1 and then the dense phase of delta[t]
   //   [cs, cs+2*st)         state helpers in two groups, one lane per state;
   //                         group g prepares step t+1 for the steps t of parity
   //                         g (certification and exact winner over d >= 1), then
-  //                         stores step t-1's results; a group has two steps for
-  //                         its work, so its serial chain overlaps the other's
+  //                         stores step t-1's results and slot t-1's messages;
+  //                         a group has two steps for its work, so its serial
+  //                         chain overlaps the other's
   //   [cs+2*st, nthr)       intake: the workers' partial winners (a lane takes
   //                         segments pk and pk + in), the emission prefix (one
   //                         lane per state), the window-sum copies and the coarse
@@ -774,7 +761,6 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   const bool is_cs = tid < cs;
   const bool is_st = !is_cs && tid < cs + 2 * st;
   const bool is_in = !is_cs && !is_st && tid < nthr;
-  const int gj = tid / G4, gl = tid % G4;              // critical: state and lane of this group
   const int sg = is_st ? (tid - cs) / st : 0;          // state helper: group (parity of its steps)
   const int sj = is_st ? (tid - cs) % st : 0;          // state helper: state
   const int pk = tid - cs - 2 * st;                    // intake: lane
@@ -846,7 +832,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
       *flag = 1;
     } else {
       const int pb = (int)(step & 1) * S;
-      take_partial(msg, seg, P.qf, pwq + pb, pwk + pb, pwd + pb, pwi + pb);
+      take_partial(msg, seg, pwq + pb, pwk + pb, pwd + pb, pwi + pb);
     }
   };
   if (T > 1) {
@@ -898,74 +884,60 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   }
   double di_cur = 0.0;  // initialisation score of step t, state tid (dense critical lanes)
   if (tid < N && 1 < D) di_cur = __ldcg(B.dinit + (size_t)1 * N + tid);
-  const int hw_chunks = L * N / 2;  // 16-byte pieces of a window-sum row
 
   int drow_prev = 0;  // (t-1) % (L+1): row of delta[t-1] in dstar_h
-  int rdrow = 1;      // t % Rd: row of delta[t] in the tagged ring
-  // Service work of the critical warps' spare lanes at step t, while the
-  // dense phase runs (all inputs are complete: slot t-1 since the dense
-  // barrier, step t-1's results since the previous step): the slot t-1
-  // messages for the workers (score, selected delta[t-1][i*], argmax word),
-  // step t-1's back-pointers and delta[t-1] in the exact ring the workers
-  // read, and the coarse base of step t+1 (max_i delta[t-1], one warp).
-  auto cs_service = [&](int sx, int ns, long long t) {
-    const int hrow = (int)((t - 1) & (L - 1));
-    const int prv = (int)((t - 1) & 1);
-    const int rprev = rdrow == 0 ? P.Rd - 1 : rdrow - 1;  // (t-1) % Rd
-    const unsigned tag = (unsigned)t;
-    for (int j = sx; j < N; j += ns) {
-      const unsigned short itv = itil_h[hrow * N + j];
-      unsigned long long* msg = B.slot_msg + ((size_t)((unsigned)(t - 1) & (SLOT_RING - 1)) * N + j) * SLOT_WORDS;
-      tagged64_store(msg, tag, (unsigned long long)ctil_h[hrow * N + j]);
-      tagged64_store(msg + 2, tag, (unsigned long long)__double_as_longlong(dstar_h[drow_prev * N + (itv & 0x7fff)]));
-      st_relaxed_u64(msg + 4, ((unsigned long long)tag << 32) | itv);
-      if (t >= 2) {
-        B.psi[(size_t)(t - 1) * N + j] = psirec[prv * N + j];
-        tagged64_store(B.dstar + ((size_t)rprev * N + j) * 2, tag,
-                       (unsigned long long)__double_as_longlong(dstar_h[drow_prev * N + j]));
-      }
-    }
-    if (sx < 32) {
-      long long mx = LLONG_MIN;
-      for (int i = sx; i < N; i += 32) mx = max(mx, dq[prv * N + i]);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-      if (sx == 0) basebuf[(int)((t + 1) & 1)] = mx;
-    }
-  };
   if (is_cs) {
-    // ================= critical warps: every step =================
+    // ================= critical lanes: every step, one lane per state =================
+    // The lane of state j computes slot t-1 of j (the matvec) and then delta[t]
+    // of j (the dense phase): neither needs another state's slot, so no barrier
+    // separates them and the slot stays in registers.
+    const int j = tid;
+    long long pfx = 0;  // P(t-1) of state j: the fixed-point emission prefix
+    long long qe_n = 0; // the prefix term of step t (added after the slot t-1)
+    int ob_n = 0;       // observation of step t+1
+    if (j < N) {
+      pfx = m.qem[(size_t)B.obs[0] * N + j];
+      if (T > 1) qe_n = m.qem[(size_t)B.obs[1] * N + j];
+      if (T > 2) ob_n = B.obs[2];
+    }
     for (long long t = 1; t < T; ++t) {
       const int cur = (int)(t & 1), prv = cur ^ 1;
       const int drow = drow_prev + 1 == L + 1 ? 0 : drow_prev + 1;  // t % (L+1)
       const int hrow = (int)((t - 1) & (L - 1));                      // slot t-1 in ctil_h
-      // ================= critical warps =================
       double di_next = 0.0;
-      if (tid < N && t + 1 < D) di_next = __ldcg(B.dinit + (size_t)(t + 1) * N + tid);
-      if (gj < N) {
-        const int j = gj;
-        // packed coarse matvec over i for slot t-1
-        int b1 = INT_MIN, b2 = INT_MIN;
+      if (j < N && t + 1 < D) di_next = __ldcg(B.dinit + (size_t)(t + 1) * N + j);
+      long long cv = 0;
+      int ifine = 0;
+      bool amb = false;
+      if (j < N) {
+        // packed coarse matvec over i for slot t-1: coarse score << 7 |
+        // (127 - i), so one integer max gives the value and the lowest index;
+        // two independent chains of (best, runner-up)
+        int b1 = INT_MIN, b2 = INT_MIN, c1 = INT_MIN, c2 = INT_MIN;
         const int* qrow = Qcp + j * Np;
         const int* dv = dqcp + prv * Np;
-        for (int i4 = gl * 4; i4 < Np; i4 += 4 * G4) {
-          const int4 a = *reinterpret_cast<const int4*>(qrow + i4);
-          const int4 b = *reinterpret_cast<const int4*>(dv + i4);
-          packed_push(a.x + b.x, b1, b2);
-          packed_push(a.y + b.y, b1, b2);
-          packed_push(a.z + b.z, b1, b2);
-          packed_push(a.w + b.w, b1, b2);
+#pragma unroll 2
+        for (int i4 = 0; i4 < Np; i4 += 8) {
+          const int4 a0 = *reinterpret_cast<const int4*>(qrow + i4);
+          const int4 d0 = *reinterpret_cast<const int4*>(dv + i4);
+          const int4 a1 = *reinterpret_cast<const int4*>(qrow + i4 + 4);
+          const int4 d1 = *reinterpret_cast<const int4*>(dv + i4 + 4);
+          packed_push(a0.x + d0.x, b1, b2);
+          packed_push(a1.x + d1.x, c1, c2);
+          packed_push(a0.y + d0.y, b1, b2);
+          packed_push(a1.y + d1.y, c1, c2);
+          packed_push(a0.z + d0.z, b1, b2);
+          packed_push(a1.z + d1.z, c1, c2);
+          packed_push(a0.w + d0.w, b1, b2);
+          packed_push(a1.w + d1.w, c1, c2);
         }
-#pragma unroll
-        for (int o = G4 / 2; o > 0; o >>= 1) {
-          const int o1 = __shfl_xor_sync(gmask, b1, o);
-          const int o2 = __shfl_xor_sync(gmask, b2, o);
-          const int lo = min(b1, o1);
-          b1 = max(b1, o1);
-          b2 = max(max(b2, o2), lo);
+        {
+          const int lo = min(b1, c1);
+          b1 = max(b1, c1);
+          b2 = max(max(b2, c2), lo);
         }
-        int ifine = 127 - (b1 & 127);
-        bool amb = ((b1 >> 7) - (b2 >> 7)) <= P.coarse_margin;
+        ifine = 127 - (b1 & 127);
+        amb = ((b1 >> 7) - (b2 >> 7)) <= P.coarse_margin;
         long long bfine;
         if (!amb) {
           bfine = qtr_at(j, ifine) + dq[prv * N + ifine];
@@ -973,86 +945,71 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
           // fine int64 pass decides (and certifies with the fine margin)
           Top2 tb;
           tb.init();
-          // (a whole row: the shared copy, else the global one, whose loads
-          // are independent and overlap, unlike N dependent conversions)
           const long long* qrow_f = P.qtr_smem ? qtr_s + (size_t)j * N : m.qtr + (size_t)j * N;
-          for (int i = gl; i < N; i += G4) tb.push(qrow_f[i] + dq[prv * N + i], i);
-#pragma unroll
-          for (int o = G4 / 2; o > 0; o >>= 1) {
-            const long long ob1 = __shfl_xor_sync(gmask, tb.b1, o);
-            const long long ob2 = __shfl_xor_sync(gmask, tb.b2, o);
-            const int ox1 = __shfl_xor_sync(gmask, tb.x1, o);
-            tb.merge(ob1, ox1, ob2);
-          }
+          for (int i = 0; i < N; ++i) tb.push(qrow_f[i] + dq[prv * N + i], i);
           ifine = tb.x1;
           bfine = tb.b1;
           amb = (tb.b1 - tb.b2) <= margin;
         }
-        if (gl == 0) {
-          ctil_h[hrow * N + j] = bfine - ptil[(int)((t - 1) & 3) * N + j];
-          itil_h[hrow * N + j] = (unsigned short)(ifine | (amb ? 0x8000 : 0));
-        }
+        cv = bfine - pfx;
+        ctil_h[hrow * N + j] = cv;
+        itil_h[hrow * N + j] = (unsigned short)(ifine | (amb ? 0x8000 : 0));
+        pfx += qe_n;  // P(t)
+        if (t + 1 < T) qe_n = m.qem[(size_t)ob_n * N + j];
+        if (t + 2 < T) ob_n = B.obs[t + 2];
       }
       named_arrive(cur ? BAR_SLOT1 : BAR_SLOT0, cs + st);  // slot t-1 ready for the group of step t
-      named_sync(BAR_DENSE, cs);                            // every state's slot t-1 is in
-      if (tid < P.cs_dense) {
-        // the winner over d >= 1 of step t, prepared by the group of step t-1
-        if (t >= 2) named_sync(prv ? BAR_PRE1 : BAR_PRE0, P.cs_dense + st);
-        if (tid < N) {
-          // dense phase, one lane per state; the exact d = 0 score of the
-          // certified argmax over i is computed before it is known to be needed
-          const int dj = tid;
-          const long long W0 = ctil_h[hrow * N + dj] + qd_h[dj * L];  // the d = 0 candidate, fixed point
-          const unsigned short it = itil_h[hrow * N + dj];
-          const long long Wt = prew[cur * N + dj];
-          const long long pk0 = prek[cur * N + dj];
-          const int pd0 = pred[cur * N + dj], pi0 = prei[cur * N + dj];
-          const long long pq0 = preq[cur * N + dj];
-          const int i1 = it & 0x7fff;
-          const double e0 = hwr[(int)(t & (HWR - 1)) * L * N + dj];
-          const double du0 = dur_h[dj * L];
-          // src/hsmm.cu:341-346 with E_t[0]
-          const double V0 = (e0 + dstar_h[drow_prev * N + i1]) + (trh[(size_t)dj * N + i1] + du0);
-          const long long q0 = fixed_from_double(V0, P.qf);
-          long long kk = pk0, fq = pq0;
-          int dd = pd0, ii = pi0;
-          if (W0 >= Wt - margin) {
-            ExactBest eb;
-            if (!(it & 0x8000)) {
-              eb.set(V0, 0, i1);
-            } else {
-              eb.init();
-              const double* row = dstar_h + drow_prev * N;
-              const double* trj = trh + (size_t)dj * N;
-              for (int i = 0; i < N; ++i) eb.offer((e0 + row[i]) + (trj[i] + du0), 0, i);
-            }
-            if (W0 <= Wt + margin) eb.offer_key(pk0, pd0, pi0);
-            kk = eb.k;
-            dd = eb.d;
-            ii = eb.i;
-            if (dd == 0) fq = (it & 0x8000) ? fixed_from_double(eb.value(), P.qf) : q0;
+      // the winner over d >= 1 of step t, prepared by the group of step t-1
+      if (t >= 2) named_sync(prv ? BAR_PRE1 : BAR_PRE0, cs + st);
+      if (j < N) {
+        // Dense phase: the d = 0 candidate's fixed-point score W0 against
+        // Wtop, the best over d >= 1 with its exact winner; the exact d = 0
+        // score of the certified argmax over i is computed before it is known
+        // to be needed.
+        const long long W0 = cv + qd_h[j * L];
+        const long long Wt = prew[cur * N + j];
+        const long long pk0 = prek[cur * N + j];
+        const int pd0 = pred[cur * N + j], pi0 = prei[cur * N + j];
+        const long long pq0 = preq[cur * N + j];
+        const double e0 = hwr[(int)(t & (HWR - 1)) * L * N + j];
+        const double du0 = dur_h[j * L];
+        // src/hsmm.cu:341-346 with E_t[0]
+        const double V0 = (e0 + dstar_h[drow_prev * N + ifine]) + (trh[(size_t)j * N + ifine] + du0);
+        const long long q0 = fixed_from_double(V0, P.qf);
+        long long kk = pk0, fq = pq0;
+        int dd = pd0, ii = pi0;
+        if (W0 >= Wt - margin) {
+          ExactBest eb;
+          if (!amb) {
+            eb.set(V0, 0, ifine);
+          } else {
+            eb.init();
+            const double* row = dstar_h + drow_prev * N;
+            const double* trj = trh + (size_t)j * N;
+            for (int i = 0; i < N; ++i) eb.offer((e0 + row[i]) + (trj[i] + du0), 0, i);
           }
-          double fin = key_value(kk);
-          uint32_t wv = pack_psi(dd, ii);
-          // t < D: the induction result replaces the initialisation score only
-          // when strictly larger (src/hsmm.cu:353-358).
-          if (t < D && !(kk > order_key(di_cur))) {
-            fin = di_cur;
-            wv = pack_psi((int)t, 0);
-            fq = fixed_from_double(fin, P.qf);
-          }
-          dstar_h[drow * N + dj] = fin;
-          dq[cur * N + dj] = fq;
-          dqcp[cur * Np + dj] = coarse_of(fq - basebuf[cur], sh) * 128;
-          psirec[cur * N + dj] = wv;
+          if (W0 <= Wt + margin) eb.offer_key(pk0, pd0, pi0);
+          kk = eb.k;
+          dd = eb.d;
+          ii = eb.i;
+          if (dd == 0) fq = amb ? fixed_from_double(eb.value(), P.qf) : q0;
         }
-        if (P.cs_dense == cs) cs_service(tid, cs, t);  // no spare warps: the dense lanes do it after
-      } else {
-        cs_service(tid - P.cs_dense, cs - P.cs_dense, t);
+        double fin = key_value(kk);
+        uint32_t wv = pack_psi(dd, ii);
+        // t < D: the induction result replaces the initialisation score only
+        // when strictly larger (src/hsmm.cu:353-358).
+        if (t < D && !(kk > order_key(di_cur))) {
+          fin = di_cur;
+          wv = pack_psi((int)t, 0);
+          fq = fixed_from_double(fin, P.qf);
+        }
+        dstar_h[drow * N + j] = fin;
+        dq[cur * N + j] = fq;
+        dqcp[cur * Np + j] = coarse_of(fq - basebuf[cur], sh) * 128;
+        psirec[(int)(t & 3) * N + j] = wv;
       }
       di_cur = di_next;
       drow_prev = drow;
-      rdrow = rdrow + 1 == P.Rd ? 0 : rdrow + 1;
       named_sync(BAR_STEP, cs + in);
       if (*(volatile int*)&s_fb[cur]) break;  // the intake failed at this step
     }
@@ -1189,7 +1146,24 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
         prei[nx * N + sj] = er.i;
         preq[nx * N + sj] = qr;
       }
-      if (next) named_arrive(sg ? BAR_PRE1 : BAR_PRE0, P.cs_dense + st);
+      if (next) named_arrive(sg ? BAR_PRE1 : BAR_PRE0, cs + st);
+      // results of step t-1, off the critical path: the slot t-1 messages
+      // for the workers (score, selected delta[t-1][i*], argmax word), the
+      // back-pointers and delta[t-1] in the exact ring the workers read
+      if (has_sj) {
+        const unsigned tag = (unsigned)t;
+        const unsigned short itv = itil_h[hrow * N + sj];
+        unsigned long long* msg =
+            B.slot_msg + ((size_t)((unsigned)(t - 1) & (SLOT_RING - 1)) * N + sj) * SLOT_WORDS;
+        tagged64_store(msg, tag, (unsigned long long)ctil_h[hrow * N + sj]);
+        tagged64_store(msg + 2, tag, (unsigned long long)__double_as_longlong(dstar_h[drw1 * N + (itv & 0x7fff)]));
+        st_relaxed_u64(msg + 4, ((unsigned long long)tag << 32) | itv);
+        if (t >= 2) {
+          B.psi[(size_t)(t - 1) * N + sj] = psirec[((ti - 1) & 3) * N + sj];
+          tagged64_store(B.dstar + ((size_t)((ti - 1) % P.Rd) * N + sj) * 2, tag,
+                         (unsigned long long)__double_as_longlong(dstar_h[drw1 * N + sj]));
+        }
+      }
     }
   } else {
     // ============ intake: every step ============
@@ -1232,6 +1206,14 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
                       (unsigned)(L * N * sizeof(double)), &s_hwbar);
         last_copy = t - 1;  // the copy's index: it completes the barrier's phase t-1
       }
+      // coarse base of step t+1: max_i delta[t-1] (the first intake warp)
+      if (pk < 32) {
+        long long mx = LLONG_MIN;
+        for (int i = pk; i < N; i += 32) mx = max(mx, dq[prv * N + i]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (pk == 0) basebuf[cur ^ 1] = mx;
+      }
       named_sync(BAR_STEP, cs + in);
       if (*(volatile int*)&s_fb[cur]) {
         // the intake failed at this step: the group of step t+1 waits for its
@@ -1262,11 +1244,11 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
     }
     named_sync(BAR_END, nthr);
     if (s_fail) return;
-    if (is_cs && gj < N) {
-      const int j = gj;
+    if (is_cs && tid < N) {
+      const int j = tid;
       ExactBest eb;
       eb.init();
-      for (int d = gl; d < hl; d += G4) {
+      for (int d = 0; d < hl; ++d) {
         const double e = hwr[((int)(t & (HWR - 1)) * L + d) * N + j] + m.survT[(size_t)j * D + d];
         // the tail reads delta[t-1-d] = delta[T-2-d]
         const int dr = (int)((T - 2 - d) % (L + 1));
@@ -1274,16 +1256,13 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
         const double* trj = trh + (size_t)j * N;
         for (int i = 0; i < N; ++i) eb.offer((e + row[i]) + trj[i], d, i);
       }
-      group_reduce_exact<G4>(eb, gmask);
-      if (gl == 0) {
-        const int a = B.seg_first[j], b = a + B.seg_count[j];
-        const int tb_ = (int)(T & 1) * S;  // the tail partials' buffer
-        for (int k = a; k < b; ++k)
-          if (pwd[tb_ + k] != EMPTY_D) eb.offer_key(pwk[tb_ + k], pwd[tb_ + k], pwi[tb_ + k]);
-        if (eb.d == IDX_NONE) { eb.d = 0; eb.i = 0; }
-        tail[j] = eb.value();
-        B.psi[(size_t)t * N + j] = pack_psi(eb.d, eb.i);
-      }
+      const int a = B.seg_first[j], b = a + B.seg_count[j];
+      const int tb_ = (int)(T & 1) * S;  // the tail partials' buffer
+      for (int k = a; k < b; ++k)
+        if (pwd[tb_ + k] != EMPTY_D) eb.offer_key(pwk[tb_ + k], pwd[tb_ + k], pwi[tb_ + k]);
+      if (eb.d == IDX_NONE) { eb.d = 0; eb.i = 0; }
+      tail[j] = eb.value();
+      B.psi[(size_t)t * N + j] = pack_psi(eb.d, eb.i);
     }
     named_sync(BAR_END, nthr);
   }
@@ -1314,12 +1293,12 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   }
 }
 
-template <bool GW, int G4>
+template <bool GW>
 __global__ void __launch_bounds__(GRID_THREADS, 1) grid_decode_kernel(ModelView m, GridParams P, GridBufs B) {
   extern __shared__ __align__(16) unsigned char smem[];
   if (ld_relaxed_i32(B.abort_flag)) return;  // rejected observations
   if (blockIdx.x == 0) {
-    grid_head<G4>(m, P, B, smem);
+    grid_head(m, P, B, smem);
   } else if (threadIdx.x < (GW ? WORKER_THREADS_GW : WORKER_THREADS) + WORKER_SERVICE) {
     grid_worker<GW>(m, P, B, smem);
   }

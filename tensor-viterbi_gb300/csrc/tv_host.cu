@@ -387,13 +387,12 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
       max_seg = std::max(max_seg, jb - ja + 1);
     }
   };
-  // Head roles: the critical warps (4 matvec lanes per state when everything
-  // fits the block, else 2), two state-helper groups of a lane per state, and
-  // intake lanes that take two segments each and cover the states.
+  // Head roles: the critical lanes and two state-helper groups, a lane per
+  // state each, and intake lanes that take two segments each and cover the
+  // states.
   auto round32 = [](int x) { return (x + 31) / 32 * 32; };
   auto intake_threads = [&](int S_) { return round32(std::max((S_ + 1) / 2, N)); };
-  auto head_threads = [&](int g4, int S_) { return round32(g4 * N) + 2 * round32(N) + intake_threads(S_); };
-  auto head_roles_fit = [&](int S_) { return head_threads(2, S_) <= tv::GRID_THREADS; };
+  auto head_roles_fit = [&](int S_) { return 3 * round32(N) + intake_threads(S_) <= tv::GRID_THREADS; };
   // Cells are split per state (row-aligned) when every state gets whole
   // workers, so that a worker's duration and transition rows are one state's;
   // otherwise in equal contiguous chunks that may span states.
@@ -468,10 +467,7 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
   o = 0;
   const int Np = (N + 15) / 16 * 16;
   P.Np = Np;
-  // 4 matvec lanes per state when the roles fit the block, else 2
-  P.head_group = head_threads(tv::HEAD_GROUP, S) <= tv::GRID_THREADS ? tv::HEAD_GROUP : 2;
-  P.cs_threads = round32(P.head_group * N);
-  P.cs_dense = round32(N);
+  P.cs_threads = round32(N);
   P.st_threads = round32(N);
   P.in_threads = intake_threads(S);
   P.block = std::max(P.cs_threads + 2 * P.st_threads + P.in_threads,
@@ -497,7 +493,7 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
   P.h_pwk = o;    o = tv::tv_align(o + (unsigned long long)2 * S * 8);
   P.h_pwd = o;    o = tv::tv_align(o + (unsigned long long)2 * S * 4);
   P.h_pwi = o;    o = tv::tv_align(o + (unsigned long long)2 * S * 4);
-  P.h_psirec = o; o = tv::tv_align(o + (unsigned long long)2 * N * 4);
+  P.h_psirec = o; o = tv::tv_align(o + (unsigned long long)4 * N * 4);
   P.h_tail = o;   o = tv::tv_align(o + (unsigned long long)N * 8);
   // The exact transition matrix and its fixed-point copy join the head's
   // shared memory when they fit; the exact one first (the fixed-point copy
@@ -514,12 +510,9 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
   return std::max(P.w_bytes, P.h_bytes) + 256 <= (unsigned long long)smem_optin;
 }
 
-// The grid kernel instance for a plan: window in shared or global memory,
-// 4 or 2 matvec lanes per state in the head.
+// The grid kernel instance for a plan: window in shared or global memory.
 const void* grid_kernel_for(const tv::GridParams& P) {
-  if (P.w_global)
-    return P.head_group == 4 ? (const void*)tv::grid_decode_kernel<true, 4> : (const void*)tv::grid_decode_kernel<true, 2>;
-  return P.head_group == 4 ? (const void*)tv::grid_decode_kernel<false, 4> : (const void*)tv::grid_decode_kernel<false, 2>;
+  return P.w_global ? (const void*)tv::grid_decode_kernel<true> : (const void*)tv::grid_decode_kernel<false>;
 }
 
 int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_dev, double* ll_dev,

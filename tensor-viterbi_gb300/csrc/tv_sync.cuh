@@ -31,44 +31,46 @@ __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned l
   asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// A message of three 64-bit words, each carrying the 32-bit step tag in its
-// high half.  Single 8-byte stores are single-copy atomic, so a reader that
-// sees the expected tag in all three words holds a consistent message
-// without any fence: one L2 round trip per message.
-constexpr int MSG_WORDS = 3;
+// A message of five 64-bit words, each carrying the 32-bit step tag in its
+// high half: two 64-bit payloads in two halves each, and a 32-bit payload.
+// Single 8-byte stores are single-copy atomic, so a reader that sees the
+// expected tag in every word holds a consistent message without any fence:
+// one L2 round trip per message.
+constexpr int MSG_WORDS = 5;
 struct TaggedMsg {
   unsigned long long w[MSG_WORDS];
 };
 
-__device__ __forceinline__ void msg_pack(TaggedMsg& m, unsigned tag, double v, int d, int i) {
-  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+__device__ __forceinline__ void msg_pack(TaggedMsg& m, unsigned tag, long long a, long long b, unsigned c) {
   const unsigned long long hi = (unsigned long long)tag << 32;
-  m.w[0] = hi | (bits & 0xffffffffull);
-  m.w[1] = hi | (bits >> 32);
-  m.w[2] = hi | ((unsigned long long)(d & 0xffff) << 16) | (unsigned long long)(i & 0xffff);
+  m.w[0] = hi | ((unsigned long long)a & 0xffffffffull);
+  m.w[1] = hi | ((unsigned long long)a >> 32);
+  m.w[2] = hi | ((unsigned long long)b & 0xffffffffull);
+  m.w[3] = hi | ((unsigned long long)b >> 32);
+  m.w[4] = hi | c;
 }
 
 __device__ __forceinline__ bool msg_tag_ok(const TaggedMsg& m, unsigned tag) {
-  return (unsigned)(m.w[0] >> 32) == tag && (unsigned)(m.w[1] >> 32) == tag && (unsigned)(m.w[2] >> 32) == tag;
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < MSG_WORDS; ++k) ok = ok && (unsigned)(m.w[k] >> 32) == tag;
+  return ok;
 }
 
-__device__ __forceinline__ void msg_unpack(const TaggedMsg& m, double& v, int& d, int& i) {
-  const unsigned long long bits = (m.w[0] & 0xffffffffull) | ((m.w[1] & 0xffffffffull) << 32);
-  v = __longlong_as_double((long long)bits);
-  d = (int)((m.w[2] >> 16) & 0xffff);
-  i = (int)(m.w[2] & 0xffff);
+__device__ __forceinline__ void msg_unpack(const TaggedMsg& m, long long& a, long long& b, unsigned& c) {
+  a = (long long)((m.w[0] & 0xffffffffull) | ((m.w[1] & 0xffffffffull) << 32));
+  b = (long long)((m.w[2] & 0xffffffffull) | ((m.w[3] & 0xffffffffull) << 32));
+  c = (unsigned)(m.w[4] & 0xffffffffull);
 }
 
 __device__ __forceinline__ void msg_store(unsigned long long* dst, const TaggedMsg& m) {
-  st_relaxed_u64(dst + 0, m.w[0]);
-  st_relaxed_u64(dst + 1, m.w[1]);
-  st_relaxed_u64(dst + 2, m.w[2]);
+#pragma unroll
+  for (int k = 0; k < MSG_WORDS; ++k) st_relaxed_u64(dst + k, m.w[k]);
 }
 
 __device__ __forceinline__ void msg_load(const unsigned long long* src, TaggedMsg& m) {
-  m.w[0] = ld_relaxed_u64(src + 0);
-  m.w[1] = ld_relaxed_u64(src + 1);
-  m.w[2] = ld_relaxed_u64(src + 2);
+#pragma unroll
+  for (int k = 0; k < MSG_WORDS; ++k) m.w[k] = ld_relaxed_u64(src + k);
 }
 
 // Poll until the message carries `tag`.  Returns false on abort / timeout.
