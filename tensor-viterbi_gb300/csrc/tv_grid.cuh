@@ -334,13 +334,22 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
   __shared__ int s_bad[2];
   const bool is_scan = tid < WT;
 
+  // Fixed-point durations below L are masked in the worker's copy: with every
+  // fixed-point score below 2^61 in magnitude, a masked cell scores below
+  // QNEG and never enters a scan's best or runner-up, so the scan needs no
+  // range test once tau = D.
+  constexpr long long QMASK = -(3LL << 61);
   if (is_scan && !GW) {
     for (long long k = tid; k < (long long)nseg * D; k += WT) {
-      qd_s[k] = m.qdurT[(size_t)ja * D + k];
+      qd_s[k] = (k % D) < L ? QMASK : m.qdurT[(size_t)ja * D + k];
       dur_s[k] = m.durT[(size_t)ja * D + k];
     }
     for (int k = tid; k < nseg * N; k += WT) tr_s[k] = m.trans[(size_t)ja * N + k];
   }
+  // Slot scores start at 0: a cell whose first slot has not arrived yet is
+  // read (masked) by the unpredicated scan, and must hold a bounded value.
+  if (is_scan)
+    for (long long k = tid; k < c_hi - c_lo; k += WT) ctil[k] = 0;
   if (tid == 0) { s_bad[0] = 0; s_bad[1] = 0; }
 
   auto seg_of = [&](int s, int& rb, int& re) {
@@ -390,15 +399,41 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
         const double* ac = accb + a3 * accs + s * D - off0;
         double* an = accb + an3 * accs + s * D - off0;
         const double em1 = fold ? emw[(int)(t1 & 1) * P.max_seg + s] : 0.0;
-        Top2 tb;
+        Top2 tb, tc;  // two independent chains, merged after the loop
         tb.init();
+        tc.init();
+        if (!GW && tau == D) {
+          // every d < D is in range; d < L is masked in the table
+          int r = rb + tid;
+          for (; r + WT < re; r += 2 * WT) {
+            int d = r0 - r;
+            if (d < 0) d += D;
+            int d2 = d - WT;
+            if (d2 < 0) d2 += D;
+            const long long v0 = ct[r] + q[d], v1 = ct[r + WT] + q[d2];
+            tb.push(v0, d);
+            tc.push(v1, d2);
+            if (fold) {
+              an[r] = ((r == r0n) ? 0.0 : ac[r]) + em1;
+              an[r + WT] = ((r + WT == r0n) ? 0.0 : ac[r + WT]) + em1;
+            }
+          }
+          if (r < re) {
+            int d = r0 - r;
+            if (d < 0) d += D;
+            tb.push(ct[r] + q[d], d);
+            if (fold) an[r] = ((r == r0n) ? 0.0 : ac[r]) + em1;
+          }
+        } else {
 #pragma unroll 4
-        for (int r = rb + tid; r < re; r += WT) {
-          int d = r0 - r;
-          if (d < 0) d += D;
-          if (d >= L && d < tau) tb.push(ct[r] + q[d], d);
-          if (fold) an[r] = ((r == r0n) ? 0.0 : ac[r]) + em1;
+          for (int r = rb + tid; r < re; r += WT) {
+            int d = r0 - r;
+            if (d < 0) d += D;
+            if (d >= L && d < tau) tb.push(ct[r] + q[d], d);
+            if (fold) an[r] = ((r == r0n) ? 0.0 : ac[r]) + em1;
+          }
         }
+        tb.merge(tc.b1, tc.x1, tc.b2);
         tb.warp_reduce();
         if (lane == 0) redb[s * NW + warp] = tb;
       }
@@ -702,7 +737,11 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const long long T = B.T;
   const long long margin = m.margin;
-  int* Qcp = (int*)(sm + P.h_qcp);                    // [N][Np] packed coarse trans
+  // [N][Qs] packed coarse trans; the row stride Qs = Np + 4 puts the 16-byte
+  // pieces that 8 consecutive states' lanes load together in 8 different
+  // bank quads (Np/4 is even, Qs/4 odd)
+  const int Qs = Np + 4;
+  int* Qcp = (int*)(sm + P.h_qcp);
   long long* qtr_s = (long long*)(sm + P.h_qtr);      // [N][N] fine trans (when it fits)
   double* trh_s = (double*)(sm + P.h_trh);            // [N][N] exact trans (when it fits)
   const double* trh = P.trans_smem ? trh_s : m.trans;
@@ -721,8 +760,8 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   long long* ctil_h = (long long*)(sm + P.h_ctil);    // [L][N]
   unsigned short* itil_h = (unsigned short*)(sm + P.h_itil);
   double* hwr = (double*)(sm + P.h_hwr);              // [HWR][L][N] window sums, row t % HWR
-  long long* qd_h = (long long*)(sm + P.h_qd);        // [N][L]
-  double* dur_h = (double*)(sm + P.h_dur);            // [N][L]
+  long long* qd_h = (long long*)(sm + P.h_qd);        // [L][N] (consecutive states, consecutive banks)
+  double* dur_h = (double*)(sm + P.h_dur);            // [L][N]
   long long* prek = (long long*)(sm + P.h_prek);      // [2][N] exact winner over d >= 1: order key
   int* pred = (int*)(sm + P.h_pred);
   int* prei = (int*)(sm + P.h_prei);
@@ -779,9 +818,9 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
     const int jj = k / Np, i = k % Np;
     if (i < N) {
       const int c = coarse_of(m.qtr[(size_t)jj * N + i], sh);
-      Qcp[k] = c * 128 + (127 - i);
+      Qcp[jj * Qs + i] = c * 128 + (127 - i);
     } else {
-      Qcp[k] = INT_MIN;
+      Qcp[jj * Qs + i] = INT_MIN;
     }
   }
   for (int k = tid; k < N * N; k += blockDim.x) {
@@ -789,7 +828,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
     if (P.trans_smem) trh_s[k] = m.trans[k];
   }
   for (int k = tid; k < N * L; k += blockDim.x) {
-    const int jj = k / L, d = k % L;
+    const int d = k / N, jj = k % N;
     qd_h[k] = m.qdurT[(size_t)jj * D + d];
     dur_h[k] = m.durT[(size_t)jj * D + d];
   }
@@ -914,7 +953,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
         // (127 - i), so one integer max gives the value and the lowest index;
         // two independent chains of (best, runner-up)
         int b1 = INT_MIN, b2 = INT_MIN, c1 = INT_MIN, c2 = INT_MIN;
-        const int* qrow = Qcp + j * Np;
+        const int* qrow = Qcp + j * Qs;
         const int* dv = dqcp + prv * Np;
 #pragma unroll 2
         for (int i4 = 0; i4 < Np; i4 += 8) {
@@ -966,13 +1005,13 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
         // Wtop, the best over d >= 1 with its exact winner; the exact d = 0
         // score of the certified argmax over i is computed before it is known
         // to be needed.
-        const long long W0 = cv + qd_h[j * L];
+        const long long W0 = cv + qd_h[j];
         const long long Wt = prew[cur * N + j];
         const long long pk0 = prek[cur * N + j];
         const int pd0 = pred[cur * N + j], pi0 = prei[cur * N + j];
         const long long pq0 = preq[cur * N + j];
         const double e0 = hwr[(int)(t & (HWR - 1)) * L * N + j];
-        const double du0 = dur_h[j * L];
+        const double du0 = dur_h[j];
         // src/hsmm.cu:341-346 with E_t[0]
         const double V0 = (e0 + dstar_h[drow_prev * N + ifine]) + (trh[(size_t)j * N + ifine] + du0);
         const long long q0 = fixed_from_double(V0, P.qf);
@@ -1047,7 +1086,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
 #pragma unroll
         for (int d = 2; d < L; ++d) {
           const int row = (ti - d) & (L - 1);
-          Wd[d] = d < hl1 ? ctil_h[row * N + sj] + qd_h[sj * L + d] : QNEG;
+          Wd[d] = d < hl1 ? ctil_h[row * N + sj] + qd_h[d * N + sj] : QNEG;
           itd[d] = itil_h[row * N + sj];
         }
         long long Wh = QNEG, W2 = QNEG;
@@ -1067,7 +1106,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
         if (dh > 0) {
           const int dr = (ti - dh) % (L + 1);  // row of delta[t-dh]
           const double e = hwr[((int)(t1 & (HWR - 1)) * L + dh) * N + sj];
-          Vh = (e + dstar_h[dr * N + ih]) + (trh[(size_t)sj * N + ih] + dur_h[sj * L + dh]);
+          Vh = (e + dstar_h[dr * N + ih]) + (trh[(size_t)sj * N + ih] + dur_h[dh * N + sj]);
           qh = fixed_from_double(Vh, P.qf);
         }
         Wr = Wh;
@@ -1097,7 +1136,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
             for (int d = 2; d < hl1; ++d) {
               if (Wd[d] < thr) continue;
               const double e = hwr[((int)(t1 & (HWR - 1)) * L + d) * N + sj];
-              const double du = dur_h[sj * L + d];
+              const double du = dur_h[d * N + sj];
               const double* drw = dstar_h + ((ti - d) % (L + 1)) * N;
               const double* trj = trh + (size_t)sj * N;
               const unsigned short it = itd[d];
@@ -1117,11 +1156,11 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
       const int drw1 = (ti - 1) % (L + 1);               // row of delta[t-1]
       if (has_sj && next) {
         // d = 1 (slot t-1): merged exactly when it is within the margin of R
-        const long long W1 = hl1 > 1 ? ctil_h[hrow * N + sj] + qd_h[sj * L + 1] : QNEG;
+        const long long W1 = hl1 > 1 ? ctil_h[hrow * N + sj] + qd_h[N + sj] : QNEG;
         const unsigned short it1 = itil_h[hrow * N + sj];
         if (hl1 > 1 && W1 >= Wr - margin) {
           const double e = hwr[((int)(t1 & (HWR - 1)) * L + 1) * N + sj];
-          const double du = dur_h[sj * L + 1];
+          const double du = dur_h[N + sj];
           const double* drw = dstar_h + drw1 * N;
           const double* trj = trh + (size_t)sj * N;
           if (!(it1 & 0x8000)) {

@@ -473,7 +473,7 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
   P.block = std::max(P.cs_threads + 2 * P.st_threads + P.in_threads,
                      (P.w_global ? tv::WORKER_THREADS_GW : tv::WORKER_THREADS) + tv::WORKER_SERVICE);
   if (P.block > tv::GRID_THREADS) return false;
-  P.h_qcp = o;    o = tv::tv_align(o + (unsigned long long)N * Np * 4);
+  P.h_qcp = o;    o = tv::tv_align(o + (unsigned long long)N * (Np + 4) * 4);  // row stride Np + 4
   P.h_dqcp = o;   o = tv::tv_align(o + (unsigned long long)2 * Np * 4);
   P.h_dq = o;     o = tv::tv_align(o + (unsigned long long)2 * N * 8);
   P.h_ptil = o;   o = tv::tv_align(o + (unsigned long long)4 * N * 8);
