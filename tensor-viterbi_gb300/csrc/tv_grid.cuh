@@ -62,7 +62,7 @@ struct GridParams {
   int w_global;                  // the window lives in global memory (L2), not in shared memory
   unsigned long long w_gstride;  // bytes of one worker's window in global memory
   // head shared-memory offsets
-  unsigned long long h_qcp, h_qtr, h_trh, h_dqcp, h_dq, h_ptil, h_base, h_dstar, h_ctil, h_itil, h_hwr, h_qd, h_dur,
+  unsigned long long h_xch, h_qcp, h_qtr, h_trh, h_dqcp, h_dq, h_ptil, h_base, h_dstar, h_ctil, h_itil, h_hwr, h_qd, h_dur,
       h_prek, h_pred, h_prei, h_prew, h_preq, h_pwq, h_pwk, h_pwd, h_pwi, h_psirec, h_tail, h_bytes;
   int trans_smem;     // the exact transition matrix is kept in the head's shared memory
   int qtr_smem;       // so is its fixed-point copy (else computed from the exact one)
@@ -72,6 +72,7 @@ struct GridParams {
   int qf;             // fraction bits of the fixed-point scores
   int Np;             // N rounded up to 16 (packed coarse matvec rows)
   int cs_threads;     // critical threads: one lane per state, N rounded up to 32
+  int cs_split;       // 1: a second warp per 32 states scans the upper half of i in the matvec
   int coarse_shift;   // fine-to-coarse right shift (f - COARSE_F)
   int coarse_margin;  // certified coarse i-margin, coarse units
   long long timeout;
@@ -655,7 +656,7 @@ constexpr int HWR = 4;  // rows of window sums kept by the head: steps t .. t+3
 // Non-aligned forms: they count threads, so a warp whose lanes took different
 // branches may arrive lane by lane.
 enum { BAR_STEP = 1, BAR_SLOT0 = 2, BAR_PW0 = 4, BAR_SLOT1 = 5, BAR_PW1 = 6, BAR_PRE0 = 7, BAR_PRE1 = 8,
-       BAR_END = 9 };
+       BAR_END = 9, BAR_PAIR0 = 10 };  // BAR_PAIR0 + k: the matvec halves of state group k (k < 4)
 __device__ __forceinline__ void named_sync(int id, int count) {
   asm volatile("barrier.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
@@ -784,6 +785,8 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   // Roles, by thread range:
   //   [0, cs)               critical: one lane per state, the matvec of slot
   //                         t-1 and then the dense phase of delta[t]
+  //   [cs, cs+csb)          (when split) the upper half of each matvec, a warp
+  //                         per 32 states, handed over through shared memory
   //   [cs, cs+2*st)         state helpers in two groups, one lane per state;
   //                         group g prepares step t+1 for the steps t of parity
   //                         g (certification and exact winner over d >= 1), then
@@ -796,13 +799,19 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   //                         base
   // Threads beyond these leave once the tables are set up.
   const int cs = P.cs_threads, st = P.st_threads, in = P.in_threads;
-  const int nthr = cs + 2 * st + in;
+  const int csb = P.cs_split ? cs : 0;
+  const int nthr = cs + csb + 2 * st + in;
   const bool is_cs = tid < cs;
-  const bool is_st = !is_cs && tid < cs + 2 * st;
-  const bool is_in = !is_cs && !is_st && tid < nthr;
-  const int sg = is_st ? (tid - cs) / st : 0;          // state helper: group (parity of its steps)
-  const int sj = is_st ? (tid - cs) % st : 0;          // state helper: state
-  const int pk = tid - cs - 2 * st;                    // intake: lane
+  const bool is_csb = !is_cs && tid < cs + csb;
+  const bool is_st = !is_cs && !is_csb && tid < cs + csb + 2 * st;
+  const bool is_in = !is_cs && !is_csb && !is_st && tid < nthr;
+  // the matvec's split point over i (a multiple of 8), and its upper half's
+  // best and runner-up per state
+  const int Nh = P.cs_split ? (Np / 16) * 8 : Np;
+  int2* xch = (int2*)(sm + P.h_xch);
+  const int sg = is_st ? (tid - cs - csb) / st : 0;    // state helper: group (parity of its steps)
+  const int sj = is_st ? (tid - cs - csb) % st : 0;    // state helper: state
+  const int pk = tid - cs - csb - 2 * st;              // intake: lane
   const bool has_sj = is_st && sj < N;
   const bool has_pk = is_in && pk < S;
   const bool has_pk2 = is_in && pk + in < S;
@@ -931,14 +940,6 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
     // of j (the dense phase): neither needs another state's slot, so no barrier
     // separates them and the slot stays in registers.
     const int j = tid;
-    long long pfx = 0;  // P(t-1) of state j: the fixed-point emission prefix
-    long long qe_n = 0; // the prefix term of step t (added after the slot t-1)
-    int ob_n = 0;       // observation of step t+1
-    if (j < N) {
-      pfx = m.qem[(size_t)B.obs[0] * N + j];
-      if (T > 1) qe_n = m.qem[(size_t)B.obs[1] * N + j];
-      if (T > 2) ob_n = B.obs[2];
-    }
     for (long long t = 1; t < T; ++t) {
       const int cur = (int)(t & 1), prv = cur ^ 1;
       const int drow = drow_prev + 1 == L + 1 ? 0 : drow_prev + 1;  // t % (L+1)
@@ -948,15 +949,16 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
       long long cv = 0;
       int ifine = 0;
       bool amb = false;
+      // packed coarse matvec over i for slot t-1: coarse score << 7 |
+      // (127 - i), so one integer max gives the value and the lowest index;
+      // two independent chains of (best, runner-up)
+      int b1 = INT_MIN, b2 = INT_MIN;
       if (j < N) {
-        // packed coarse matvec over i for slot t-1: coarse score << 7 |
-        // (127 - i), so one integer max gives the value and the lowest index;
-        // two independent chains of (best, runner-up)
-        int b1 = INT_MIN, b2 = INT_MIN, c1 = INT_MIN, c2 = INT_MIN;
+        int c1 = INT_MIN, c2 = INT_MIN;
         const int* qrow = Qcp + j * Qs;
         const int* dv = dqcp + prv * Np;
 #pragma unroll 2
-        for (int i4 = 0; i4 < Np; i4 += 8) {
+        for (int i4 = 0; i4 < Nh; i4 += 8) {
           const int4 a0 = *reinterpret_cast<const int4*>(qrow + i4);
           const int4 d0 = *reinterpret_cast<const int4*>(dv + i4);
           const int4 a1 = *reinterpret_cast<const int4*>(qrow + i4 + 4);
@@ -970,10 +972,17 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
           packed_push(a0.w + d0.w, b1, b2);
           packed_push(a1.w + d1.w, c1, c2);
         }
-        {
-          const int lo = min(b1, c1);
-          b1 = max(b1, c1);
-          b2 = max(max(b2, c2), lo);
+        const int lo = min(b1, c1);
+        b1 = max(b1, c1);
+        b2 = max(max(b2, c2), lo);
+      }
+      if (P.cs_split) named_sync(BAR_PAIR0 + (tid >> 5), 64);  // the upper half of this warp's states is in
+      if (j < N) {
+        if (P.cs_split) {
+          const int2 o = xch[j];
+          const int lo = min(b1, o.x);
+          b1 = max(b1, o.x);
+          b2 = max(max(b2, o.y), lo);
         }
         ifine = 127 - (b1 & 127);
         amb = ((b1 >> 7) - (b2 >> 7)) <= P.coarse_margin;
@@ -990,12 +999,9 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
           bfine = tb.b1;
           amb = (tb.b1 - tb.b2) <= margin;
         }
-        cv = bfine - pfx;
+        cv = bfine - ptil[(int)((t - 1) & 3) * N + j];  // relative to the emission prefix P(t-1)
         ctil_h[hrow * N + j] = cv;
         itil_h[hrow * N + j] = (unsigned short)(ifine | (amb ? 0x8000 : 0));
-        pfx += qe_n;  // P(t)
-        if (t + 1 < T) qe_n = m.qem[(size_t)ob_n * N + j];
-        if (t + 2 < T) ob_n = B.obs[t + 2];
       }
       named_arrive(cur ? BAR_SLOT1 : BAR_SLOT0, cs + st);  // slot t-1 ready for the group of step t
       // the winner over d >= 1 of step t, prepared by the group of step t-1
@@ -1049,7 +1055,38 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
       }
       di_cur = di_next;
       drow_prev = drow;
-      named_sync(BAR_STEP, cs + in);
+      named_sync(BAR_STEP, cs + csb + in);
+      if (*(volatile int*)&s_fb[cur]) break;  // the intake failed at this step
+    }
+  } else if (is_csb) {
+    // ============ upper half of the matvec: every step, one lane per state ============
+    const int jb = tid - cs;
+    for (long long t = 1; t < T; ++t) {
+      const int cur = (int)(t & 1), prv = cur ^ 1;
+      if (jb < N) {
+        int b1 = INT_MIN, b2 = INT_MIN, c1 = INT_MIN, c2 = INT_MIN;
+        const int* qrow = Qcp + jb * Qs;
+        const int* dv = dqcp + prv * Np;
+#pragma unroll 2
+        for (int i4 = Nh; i4 < Np; i4 += 8) {
+          const int4 a0 = *reinterpret_cast<const int4*>(qrow + i4);
+          const int4 d0 = *reinterpret_cast<const int4*>(dv + i4);
+          const int4 a1 = *reinterpret_cast<const int4*>(qrow + i4 + 4);
+          const int4 d1 = *reinterpret_cast<const int4*>(dv + i4 + 4);
+          packed_push(a0.x + d0.x, b1, b2);
+          packed_push(a1.x + d1.x, c1, c2);
+          packed_push(a0.y + d0.y, b1, b2);
+          packed_push(a1.y + d1.y, c1, c2);
+          packed_push(a0.z + d0.z, b1, b2);
+          packed_push(a1.z + d1.z, c1, c2);
+          packed_push(a0.w + d0.w, b1, b2);
+          packed_push(a1.w + d1.w, c1, c2);
+        }
+        const int lo = min(b1, c1);
+        xch[jb] = make_int2(max(b1, c1), max(max(b2, c2), lo));
+      }
+      named_arrive(BAR_PAIR0 + (jb >> 5), 64);
+      named_sync(BAR_STEP, cs + csb + in);
       if (*(volatile int*)&s_fb[cur]) break;  // the intake failed at this step
     }
   } else if (is_st) {
@@ -1213,20 +1250,9 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
       const int cur = (int)(t & 1), prv = cur ^ 1;
       // worker partials of step t+1 (loaded during the previous step) into buffer (t+1) & 1
       if (next) {
-        if (has_pk) {
-          intake_one(pk, pm, t1, SITE_HEAD_PARTIAL, &s_fb[cur]);
-          if (t1 + 1 < T) msg_load(B.part + ((size_t)((unsigned)(t1 + 1) & (PART_RING - 1)) * S + pk) * MSG_WORDS, pm);
-        }
-        if (has_pk2) {
-          intake_one(pk + in, pm2, t1, SITE_HEAD_PARTIAL, &s_fb[cur]);
-          if (t1 + 1 < T)
-            msg_load(B.part + ((size_t)((unsigned)(t1 + 1) & (PART_RING - 1)) * S + pk + in) * MSG_WORDS, pm2);
-        }
-        if (has_pj) {
-          ptil[(int)(t1 & 3) * N + pk] = ptil[(int)(t & 3) * N + pk] + qe_pf;  // P(t+1)
-          if (t + 2 < T) qe_pf = m.qem[(size_t)ob_q * N + pk];
-          if (t + 3 < T) ob_q = B.obs[t + 3];
-        }
+        if (has_pk) intake_one(pk, pm, t1, SITE_HEAD_PARTIAL, &s_fb[cur]);
+        if (has_pk2) intake_one(pk + in, pm2, t1, SITE_HEAD_PARTIAL, &s_fb[cur]);
+        if (has_pj) ptil[(int)(t1 & 3) * N + pk] = ptil[(int)(t & 3) * N + pk] + qe_pf;  // P(t+1)
       }
       // the window sums of step t+2 (copied during the previous step) are in
       // before the group of step t+1 is released
@@ -1239,6 +1265,19 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
         }
       }
       named_arrive(cur ? BAR_PW1 : BAR_PW0, st + in);
+      // loads for the next step, issued once the state helpers are released:
+      // the partials of step t+2, the prefix term of step t+2, the
+      // observation of step t+3
+      if (next) {
+        if (has_pk && t1 + 1 < T)
+          msg_load(B.part + ((size_t)((unsigned)(t1 + 1) & (PART_RING - 1)) * S + pk) * MSG_WORDS, pm);
+        if (has_pk2 && t1 + 1 < T)
+          msg_load(B.part + ((size_t)((unsigned)(t1 + 1) & (PART_RING - 1)) * S + pk + in) * MSG_WORDS, pm2);
+        if (has_pj) {
+          if (t + 2 < T) qe_pf = m.qem[(size_t)ob_q * N + pk];
+          if (t + 3 < T) ob_q = B.obs[t + 3];
+        }
+      }
       // window sums of step t+3 into the ring: one bulk copy
       if (pk == 0 && t + 3 < T) {
         bulk_copy_g2s(hwr + (int)((t + 3) & (HWR - 1)) * L * N, B.hwin + (size_t)(t + 3) * L * N,
@@ -1253,7 +1292,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
         for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         if (pk == 0) basebuf[cur ^ 1] = mx;
       }
-      named_sync(BAR_STEP, cs + in);
+      named_sync(BAR_STEP, cs + csb + in);
       if (*(volatile int*)&s_fb[cur]) {
         // the intake failed at this step: the group of step t+1 waits for its
         // partials; wake it with the notice that the loops end here

@@ -470,9 +470,13 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
   P.cs_threads = round32(N);
   P.st_threads = round32(N);
   P.in_threads = intake_threads(S);
-  P.block = std::max(P.cs_threads + 2 * P.st_threads + P.in_threads,
+  // a second warp per 32 states for the upper half of the matvec, when the
+  // block has room for it (at most 4 pairs: named barriers 10..13)
+  P.cs_split = (4 * round32(N) + P.in_threads <= tv::GRID_THREADS && round32(N) <= 128) ? 1 : 0;
+  P.block = std::max(P.cs_threads * (1 + P.cs_split) + 2 * P.st_threads + P.in_threads,
                      (P.w_global ? tv::WORKER_THREADS_GW : tv::WORKER_THREADS) + tv::WORKER_SERVICE);
   if (P.block > tv::GRID_THREADS) return false;
+  P.h_xch = o;    o = tv::tv_align(o + (unsigned long long)N * 8);
   P.h_qcp = o;    o = tv::tv_align(o + (unsigned long long)N * (Np + 4) * 4);  // row stride Np + 4
   P.h_dqcp = o;   o = tv::tv_align(o + (unsigned long long)2 * Np * 4);
   P.h_dq = o;     o = tv::tv_align(o + (unsigned long long)2 * N * 8);
