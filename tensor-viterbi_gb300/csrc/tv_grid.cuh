@@ -1003,7 +1003,9 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
         ctil_h[hrow * N + j] = cv;
         itil_h[hrow * N + j] = (unsigned short)(ifine | (amb ? 0x8000 : 0));
       }
-      named_arrive(cur ? BAR_SLOT1 : BAR_SLOT0, cs + st);  // slot t-1 ready for the group of step t
+      // slot t-1 ready for the group of step t (its d = 1) and the group of
+      // step t+1 (its d >= 2)
+      named_arrive(cur ? BAR_SLOT1 : BAR_SLOT0, t + 1 < T ? cs + 2 * st : cs + st);
       // the winner over d >= 1 of step t, prepared by the group of step t-1
       if (t >= 2) named_sync(prv ? BAR_PRE1 : BAR_PRE0, cs + st);
       if (j < N) {
@@ -1096,38 +1098,27 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
       const bool next = t1 < T;
       const int ti = (int)t;
       const int bw = (int)(t1 & 1) * S;  // partial buffer of step t+1
-      named_sync(sg ? BAR_PW1 : BAR_PW0, st + in);  // partials of step t+1, P(t+1), window sums of t+1 are in
-      const int fb = *(volatile int*)&s_fb[sg];
-      if (fb == 2) break;  // the loops ended at step t-1
-      if (fb == 1) {       // the intake failed at this step: the critical warps finish it, then leave
-        named_sync(sg ? BAR_SLOT1 : BAR_SLOT0, cs + st);
-        break;
-      }
+      const int own_cnt = next ? cs + 2 * st : cs + st;  // slot t-1 is also awaited by the group of step t+1
       // Every candidate d >= 1 of step t+1 in fixed point: d = 1..L-1 here
       // (slots t-d), d >= L as the workers' winners, whose fixed-point scores
-      // are their values minus the prefix P(t+1).  Only d = 1 needs slot t-1,
-      // which the critical warps are computing meanwhile: the rest (R) is
-      // certified first, with the exact winner among R within the margin of
-      // R's best, and the exact score of the best short candidate computed
-      // before it is known to be needed.
+      // are their values minus the prefix P(t+1).  The slots t-2..t-L+1 are in
+      // once the critical lanes published slot t-2 (their step t-1): their
+      // best and runner-up come first, before the partials arrive.  Only d = 1
+      // needs slot t-1, which the critical lanes compute meanwhile.
+      if (t >= 2) named_sync(((t - 1) & 1) ? BAR_SLOT1 : BAR_SLOT0, cs + 2 * st);
       const int tau1 = (int)(t1 < D ? t1 : D);
       const int hl1 = tau1 < L ? tau1 : L;
-      long long Wr = QNEG;
-      ExactBest er;
-      er.init();
-      long long qr = 0;
+      long long Wd[L];
+      unsigned short itd[L];
+      long long Wh = QNEG, W2 = QNEG;
+      int dh = 0, ih = 0, hamb = 0;
       if (has_sj && next) {
-        const long long p1 = ptil[(int)(t1 & 3) * N + sj];
-        long long Wd[L];
-        unsigned short itd[L];
 #pragma unroll
         for (int d = 2; d < L; ++d) {
           const int row = (ti - d) & (L - 1);
           Wd[d] = d < hl1 ? ctil_h[row * N + sj] + qd_h[d * N + sj] : QNEG;
           itd[d] = itil_h[row * N + sj];
         }
-        long long Wh = QNEG, W2 = QNEG;
-        int dh = 0, ih = 0, hamb = 0;
 #pragma unroll
         for (int d = 2; d < L; ++d) {
           W2 = max(W2, min(Wh, Wd[d]));
@@ -1138,6 +1129,23 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
             hamb = itd[d] & 0x8000;
           }
         }
+      }
+      named_sync(sg ? BAR_PW1 : BAR_PW0, st + in);  // partials of step t+1, P(t+1), window sums of t+1 are in
+      const int fb = *(volatile int*)&s_fb[sg];
+      if (fb == 2) break;  // the loops ended at step t-1
+      if (fb == 1) {       // the intake failed at this step: the critical warps finish it, then leave
+        named_sync(sg ? BAR_SLOT1 : BAR_SLOT0, own_cnt);
+        break;
+      }
+      // the exact winner among the candidates within the margin of the best
+      // over d >= 2, with the exact score of the best short candidate computed
+      // before it is known to be needed
+      long long Wr = QNEG;
+      ExactBest er;
+      er.init();
+      long long qr = 0;
+      if (has_sj && next) {
+        const long long p1 = ptil[(int)(t1 & 3) * N + sj];
         double Vh = 0.0;
         long long qh = 0;
         if (dh > 0) {
@@ -1188,7 +1196,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
           }
         }
       }
-      named_sync(sg ? BAR_SLOT1 : BAR_SLOT0, cs + st);  // the critical warps published slot t-1
+      named_sync(sg ? BAR_SLOT1 : BAR_SLOT0, own_cnt);  // the critical lanes published slot t-1
       const int hrow = (ti - 1) & (L - 1);               // slot t-1
       const int drw1 = (ti - 1) % (L + 1);               // row of delta[t-1]
       if (has_sj && next) {
