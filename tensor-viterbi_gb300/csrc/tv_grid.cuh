@@ -626,28 +626,28 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
 //
 // The serial critical path of a step is: delta[t-1] final -> B[t-1][j] =
 // max_i(trans[j][i] + delta[t-1][i]) for every j -> the d = 0 candidate ->
-// merge -> delta[t].  Only that chain runs in the critical warps:
-//   * the matvec, 4 lanes per state, in packed int32: coarse score << 7 |
-//     (127 - i), so one integer max yields the value and the lowest index;
-//     its runner-up gap is certified against a coarse margin, else a fine
+// merge -> delta[t].  Only that chain runs in the critical lanes, one per
+// state:
+//   * the matvec in packed int32: coarse score << 7 | (127 - i), so one
+//     integer max yields the value and the lowest index; a second warp per 32
+//     states scans the upper half of i and hands its best and runner-up over;
+//     the runner-up gap is certified against a coarse margin, else a fine
 //     int64 pass decides;
-//   * then one lane per state (the dense phase): the d = 0 candidate's
-//     fixed-point score W0 against Wtop, the best fixed-point score over
-//     d >= 1 that the helpers prepared one step ahead with the exact winner
-//     among d >= 1.  When W0 trails Wtop by more than the certified margin,
-//     delta[t] is that winner and no floating-point operation runs; otherwise
-//     the d = 0 score is computed exactly (two dependent FP64 adds) and
-//     compared.
+//   * then, in the same lane (no other state's slot is needed), the dense
+//     phase: the d = 0 candidate's fixed-point score W0 against Wtop, the best
+//     fixed-point score over d >= 1 that the helpers prepared with the exact
+//     winner among d >= 1.  When W0 trails Wtop by more than the certified
+//     margin, delta[t] is that winner; otherwise the d = 0 score, computed
+//     exactly (two dependent FP64 adds) ahead of the test, is compared.
 // FP64 instructions cost the same pipe time whatever the number of active
-// lanes, so exact scores are computed one lane per state, never one lane in
-// four.
-// The helper warps (the rest of the CTA) prepare step t+1 meanwhile: intake
-// of the workers' partial winners (loaded a step ahead), window sums (copied
-// asynchronously three steps ahead from a table built before the launch),
-// the candidates d = 1..L-1 in fixed point, certification, and in a dense
-// phase the exact score of the winner when it is one of them; also all global
-// stores.  A named barrier hands the matvec result (slot t-1) from the
-// critical warps to the helpers inside the step.
+// lanes, so exact scores are computed one lane per state in dense warps.
+// The helpers prepare the next steps meanwhile: the intake of the workers'
+// partial winners (loaded a step ahead), window sums (bulk-copied three steps
+// ahead from a table built before the launch), and in two alternating groups
+// the candidates d = 1..L-1 in fixed point, certification, the exact score of
+// the winner when it is one of them, and all global stores.  Named barriers
+// hand slot t-1 from the critical lanes to the helpers and the prepared
+// winner back.
 // ---------------------------------------------------------------------------
 constexpr int HWR = 4;  // rows of window sums kept by the head: steps t .. t+3
 
