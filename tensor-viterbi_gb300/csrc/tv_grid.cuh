@@ -61,6 +61,7 @@ struct GridParams {
   unsigned long long w_qd, w_dur, w_tr, w_ctil, w_dsel, w_acc, w_accs, w_itil, w_red, w_emw, w_bytes;
   int w_global;                  // the window lives in global memory (L2), not in shared memory
   unsigned long long w_gstride;  // bytes of one worker's window in global memory
+  int w_qd_smem;                 // window in global memory, fixed-point duration rows in shared memory
   // head shared-memory offsets
   unsigned long long h_xch, h_qcp, h_qtr, h_trh, h_dqcp, h_dq, h_ptil, h_base, h_dstar, h_ctil, h_itil, h_hwr, h_qd, h_dur,
       h_prek, h_pred, h_prei, h_prew, h_preq, h_pwq, h_pwk, h_pwd, h_pwi, h_psirec, h_tail, h_bytes;
@@ -318,7 +319,8 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
   long long* qd_s = (long long*)(sm + P.w_qd);        // [nseg][D]
   double* dur_s = (double*)(sm + P.w_dur);            // [nseg][D]
   double* tr_s = (double*)(sm + P.w_tr);              // [nseg][N]
-  const long long* qd = GW ? m.qdurT + (size_t)ja * D : qd_s;
+  const bool qd_in_smem = !GW || P.w_qd_smem;
+  const long long* qd = qd_in_smem ? qd_s : m.qdurT + (size_t)ja * D;
   const double* dur = GW ? m.durT + (size_t)ja * D : dur_s;
   const double* tr = GW ? m.trans + (size_t)ja * N : tr_s;
   long long* ctil = (long long*)(wb + P.w_ctil);      // [ncell]
@@ -340,11 +342,10 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
   // QNEG and never enters a scan's best or runner-up, so the scan needs no
   // range test once tau = D.
   constexpr long long QMASK = -(3LL << 61);
+  if (is_scan && qd_in_smem)
+    for (long long k = tid; k < (long long)nseg * D; k += WT) qd_s[k] = (k % D) < L ? QMASK : m.qdurT[(size_t)ja * D + k];
   if (is_scan && !GW) {
-    for (long long k = tid; k < (long long)nseg * D; k += WT) {
-      qd_s[k] = (k % D) < L ? QMASK : m.qdurT[(size_t)ja * D + k];
-      dur_s[k] = m.durT[(size_t)ja * D + k];
-    }
+    for (long long k = tid; k < (long long)nseg * D; k += WT) dur_s[k] = m.durT[(size_t)ja * D + k];
     for (int k = tid; k < nseg * N; k += WT) tr_s[k] = m.trans[(size_t)ja * N + k];
   }
   // Slot scores start at 0: a cell whose first slot has not arrived yet is
@@ -403,9 +404,10 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
         Top2 tb, tc;  // two independent chains, merged after the loop
         tb.init();
         tc.init();
-        if (!GW && tau == D) {
+        if (qd_in_smem && tau == D) {
           // every d < D is in range; d < L is masked in the table
           int r = rb + tid;
+#pragma unroll 2
           for (; r + WT < re; r += 2 * WT) {
             int d = r0 - r;
             if (d < 0) d += D;

@@ -460,6 +460,15 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
     P.w_itil = g; g = tv::tv_align(g + (unsigned long long)chunk * 2);
     P.w_gstride = (g + 255) / 256 * 256;
     P.w_qd = P.w_dur = P.w_tr = 0;
+    // The fixed-point duration rows, read every step by the scan, join shared
+    // memory when they fit.
+    const unsigned long long qbytes = tv::tv_align((unsigned long long)max_seg * D * 8);
+    if (qbytes + red_bytes(tv::WORKER_THREADS_GW / 32) + 2 * (unsigned long long)max_seg * 8 + 512 <=
+        (unsigned long long)smem_optin) {
+      P.w_qd_smem = 1;
+      P.w_qd = 0;
+      o = qbytes;
+    }
     P.w_red = o;  o = tv::tv_align(o + red_bytes(tv::WORKER_THREADS_GW / 32));
     P.w_emw = o;  o = tv::tv_align(o + (unsigned long long)2 * max_seg * 8);
     P.w_bytes = o;
