@@ -113,11 +113,29 @@ def test_grid_window_in_l2_golden(tvlib, name, grid_ctas):
     assert ll == ref["loglik"]
 
 
-def test_grid_large_n_two_lane_head(tvlib):
-    """N = 100: the head's matvec runs two lanes per state (four do not fit the
-    block beside the other roles); both window placements."""
+def test_grid_large_n_head(tvlib):
+    """N = 100: four pairs of critical and upper-half matvec warps beside the
+    other roles; both window placements."""
     import tensor_viterbi.synthetic as syn
     p = syn.discrete_problem(100, 40, 700, 24, 5.0, 30.0, seed=11)
+    ref = orc.decode(*p.args(), variant="omp")
+    with tvlib.Model(*p.model_args()) as m:
+        for kind in ("grid", "grid-l2"):
+            m.set_path(kind, 0)
+            path, ll = m.decode(p.obs_seq, return_loglik=True)
+            assert m.last_path() == "grid"
+            np.testing.assert_array_equal(path, ref["path"])
+            assert ll == ref["loglik"]
+
+
+def test_grid_max_n_head_with_and_without_split_matvec(tvlib):
+    """N = 128, the largest the packed coarse scores take.  With the window in
+    shared memory each state is one worker's segment and the upper half of the
+    matvec has its own warps; with the window in L2 the contiguous chunks give
+    more segments than the block has room for beside a split matvec, so the
+    critical lanes scan whole rows."""
+    import tensor_viterbi.synthetic as syn
+    p = syn.discrete_problem(128, 40, 700, 24, 5.0, 30.0, seed=13)
     ref = orc.decode(*p.args(), variant="omp")
     with tvlib.Model(*p.model_args()) as m:
         for kind in ("grid", "grid-l2"):
