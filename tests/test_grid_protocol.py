@@ -1,0 +1,296 @@
+"""A CPU model of the grid head's step protocol (tv_grid.cuh, grid_head).
+
+The head CTA runs five roles that meet at named non-aligned barriers:
+  * critical lanes: the matvec of slot t-1, then the dense phase of delta[t];
+  * upper-half matvec warps: hand their half over at a pair barrier;
+  * two state-helper groups: group g prepares step t+1 for the steps t of
+    parity g (short candidates after slot t-2, partials after PW, d = 1
+    after slot t-1), then stores step t-1's results;
+  * intake: worker partials, the emission prefix, window-sum copies three
+    steps ahead, the coarse base.
+
+The model runs each role as two actors (warp subsets) under random
+interleavings.  A barrier counts arrivals and completes a generation when the
+count is reached; a sync blocks until its generation completes.  Every shared
+buffer carries the step whose value it holds; every read checks that it sees
+the step it needs and that no asynchronous copy into it is in flight.  The
+checks: no deadlock, no barrier over-arrival or count mismatch, no stale or
+torn read, every barrier left empty, and after an injected intake failure
+all roles leave the step loops at the same step (the kernel's exit protocol
+through the two flag words s_fb).
+
+The model is test infrastructure: it restates the kernel's ordering argument
+so that a change to the protocol can be checked here before it runs on a GPU.
+"""
+from __future__ import annotations
+
+import random
+
+import pytest
+
+L = 8
+
+# barrier ids as in tv_grid.cuh
+STEP, SLOT0, PW0, SLOT1, PW1, PRE0, PRE1, END, PAIR0 = 1, 2, 4, 5, 6, 7, 8, 9, 10
+
+
+def SLOT(g):
+    return SLOT1 if g else SLOT0
+
+
+def PW(g):
+    return PW1 if g else PW0
+
+
+def PRE(g):
+    return PRE1 if g else PRE0
+
+
+class _Deadlock(Exception):
+    pass
+
+
+class _Bar:
+    def __init__(self):
+        self.count, self.expect, self.gen = 0, None, 0
+
+
+def run_protocol(T, D, fail_at, seed, mutate=None):
+    """Run one interleaving; return the list of violations found."""
+    rnd = random.Random(seed)
+    cs = st = inn = 4          # threads per role (two actors of 2)
+    nthr = 2 * cs + 2 * st + inn
+    bars, mem, inflight, errs, exits = {}, {}, set(), [], {}
+    s_fb = [0, 0]
+
+    def bar(i):
+        return bars.setdefault(i, _Bar())
+
+    def W(key, ver):
+        mem[key] = ver
+
+    def R(who, key, ver):
+        if key in inflight:
+            errs.append(f"{who}: read {key} while a copy into it is in flight")
+        elif mem.get(key) != ver:
+            errs.append(f"{who}: read {key} holds step {mem.get(key)}, needs {ver}")
+
+    def arrive(i, n, cnt):
+        b = bar(i)
+        if b.expect is None:
+            b.expect = cnt
+        elif b.expect != cnt:
+            errs.append(f"barrier {i}: count {cnt} against {b.expect}")
+        b.count += n
+        if b.count > b.expect:
+            errs.append(f"barrier {i}: over-arrival")
+        if b.count >= b.expect:
+            b.count, b.expect, b.gen = 0, None, b.gen + 1
+        return ("go",)
+
+    def sync(i, n, cnt):
+        g0 = bar(i).gen
+        arrive(i, n, cnt)
+        return ("wait", i, g0)
+
+    # set-up (all threads, before the first CTA-wide barrier)
+    W(("ptil", 0), 0)
+    if T > 1:
+        W(("ptil", 1), 1)
+    for r in range(4):
+        if r < T:
+            W(("hwr", r), r)
+    W(("dstar", 0), 0)
+    W(("dq", 0), 0)
+    W(("dqcp", 0), 0)
+    W(("base", 0), 0)
+    W(("base", 1), 1)
+    if T > 1:
+        W(("pw", 1), 1)
+    W(("pre", 1), 1)
+
+    def critical(name, n, k):
+        for t in range(1, T):
+            cur, prv = t & 1, (t & 1) ^ 1
+            R(name, ("dqcp", prv), t - 1)
+            R(name, ("ptil", (t - 1) & 3), t - 1)
+            if mutate != "no_pair":
+                yield sync(PAIR0 + k, n, 2 * n)
+            R(name, ("xch", k), t)
+            W(("slot", (t - 1) & 7), t - 1)
+            yield arrive(SLOT(cur), n, cs + 2 * st if t + 1 < T else cs + st)
+            if t >= 2 and mutate != "no_pre":
+                yield sync(PRE(prv), n, cs + st)
+            R(name, ("pre", cur), t)
+            R(name, ("hwr", t & 3), t)
+            R(name, ("dstar", (t - 1) % (L + 1)), t - 1)
+            R(name, ("base", cur), t)
+            W(("dstar", t % (L + 1)), t)
+            W(("dq", cur), t)
+            W(("dqcp", cur), t)
+            W(("psirec", t & 3), t)
+            yield sync(STEP, n, 2 * cs + inn)
+            if s_fb[cur]:
+                exits[name] = t
+                break
+        yield sync(END, n, nthr)
+        yield ("done",)
+
+    def upper_half(name, n, k):
+        for t in range(1, T):
+            cur, prv = t & 1, (t & 1) ^ 1
+            R(name, ("dqcp", prv), t - 1)
+            W(("xch", k), t)
+            yield arrive(PAIR0 + k, n, 2 * n)
+            yield sync(STEP, n, 2 * cs + inn)
+            if s_fb[cur]:
+                exits[name] = t
+                break
+        yield sync(END, n, nthr)
+        yield ("done",)
+
+    def helper(name, n, g):
+        t = 1 if g else 2
+        while t < T:
+            t1 = t + 1
+            nxt = t1 < T
+            hl1 = min(t1, D, L)
+            own = cs + 2 * st if nxt else cs + st
+            if t >= 2 and mutate != "no_early_slot":
+                yield sync(SLOT((t - 1) & 1), n, cs + 2 * st)
+            if nxt:
+                for d in range(2, hl1):
+                    R(name, ("slot", (t - d) & 7), t - d)
+            yield sync(PW(g), n, st + inn)
+            fb = s_fb[g]
+            if fb == 2:
+                exits[name] = t
+                break
+            if fb == 1:
+                yield sync(SLOT(g), n, own)
+                exits[name] = t
+                break
+            if nxt:
+                R(name, ("ptil", t1 & 3), t1)
+                R(name, ("pw", t1 & 1), t1)
+                R(name, ("hwr", t1 & 3), t1)
+                for d in range(2, hl1):
+                    R(name, ("dstar", (t - d) % (L + 1)), t - d)
+            yield sync(SLOT(g), n, own)
+            if nxt:
+                if hl1 > 1:
+                    R(name, ("slot", (t - 1) & 7), t - 1)
+                    R(name, ("dstar", (t - 1) % (L + 1)), t - 1)
+                    R(name, ("hwr", t1 & 3), t1)
+                W(("pre", t1 & 1), t1)
+                yield arrive(PRE(g), n, cs + st)
+            R(name, ("slot", (t - 1) & 7), t - 1)
+            R(name, ("dstar", (t - 1) % (L + 1)), t - 1)
+            if t >= 2:
+                R(name, ("psirec", (t - 1) & 3), t - 1)
+            t += 2
+        yield sync(END, n, nthr)
+        yield ("done",)
+
+    def intake(name, n, fails):
+        pending = []  # the window-sum copy in flight
+        for t in range(1, T):
+            t1 = t + 1
+            nxt = t1 < T
+            cur, prv = t & 1, (t & 1) ^ 1
+            if nxt:
+                if fails and t == fail_at:
+                    s_fb[cur] = 1
+                W(("pw", t1 & 1), t1)
+                R(name, ("ptil", t & 3), t)
+                W(("ptil", t1 & 3), t1)
+            if mutate != "no_copy_wait":
+                while pending:  # the copy issued at the previous step is complete before PW
+                    key, v = pending.pop()
+                    inflight.discard(key)
+                    W(key, v)
+            yield arrive(PW(cur), n, st + inn)
+            if t + 3 < T:
+                key = ("hwr", (t + 3) & 3)
+                inflight.add(key)
+                pending.append((key, t + 3))
+            R(name, ("dq", prv), t - 1)
+            W(("base", cur ^ 1), t1)
+            yield sync(STEP, n, 2 * cs + inn)
+            if s_fb[cur]:
+                s_fb[prv] = 2
+                yield arrive(PW(prv), n, st + inn)
+                exits[name] = t
+                break
+        for key, v in pending:
+            inflight.discard(key)
+            W(key, v)
+        yield sync(END, n, nthr)
+        yield ("done",)
+
+    actors = {
+        "crit0": critical("crit0", cs // 2, 0), "crit1": critical("crit1", cs // 2, 1),
+        "upper0": upper_half("upper0", cs // 2, 0), "upper1": upper_half("upper1", cs // 2, 1),
+        "g0a": helper("g0a", st // 2, 0), "g0b": helper("g0b", st // 2, 0),
+        "g1a": helper("g1a", st // 2, 1), "g1b": helper("g1b", st // 2, 1),
+        "in_a": intake("in_a", inn // 2, True), "in_b": intake("in_b", inn // 2, False),
+    }
+    waiting = {k: None for k in actors}
+    done = set()
+    for _ in range(10 ** 6):
+        if len(done) == len(actors):
+            break
+        ready = [k for k in actors if k not in done and
+                 (waiting[k] is None or bars[waiting[k][1]].gen > waiting[k][2])]
+        if not ready:
+            raise _Deadlock(", ".join(f"{k} at barrier {waiting[k][1]}" for k in actors if k not in done))
+        k = rnd.choice(ready)
+        waiting[k] = None
+        op = next(actors[k])
+        if op[0] == "wait":
+            waiting[k] = op
+        elif op[0] == "done":
+            done.add(k)
+    else:
+        raise _Deadlock("no progress")
+    loop_roles = ("crit0", "crit1", "upper0", "upper1", "in_a", "in_b")
+    if fail_at is not None and fail_at + 1 < T:
+        for k in loop_roles:
+            if exits.get(k) != fail_at:
+                errs.append(f"{k} left the loops at step {exits.get(k)}, not at the failed step {fail_at}")
+    elif exits:
+        errs.append(f"unexpected early exits {exits}")
+    for i, b in bars.items():
+        if b.count:
+            errs.append(f"barrier {i} left with {b.count} arrivals")
+    return errs
+
+
+def _violations(T, D, fail_at, seeds, mutate=None):
+    out = []
+    for seed in seeds:
+        try:
+            out += run_protocol(T, D, fail_at, seed, mutate)
+        except _Deadlock as e:
+            out.append(f"deadlock: {e}")
+    return out
+
+
+@pytest.mark.parametrize("T", [1, 2, 3, 4, 5, 7, 10, 13, 40])
+@pytest.mark.parametrize("D", [1, 2, 3, 9, 20])
+def test_head_protocol_runs_clean(T, D):
+    """Every interleaving completes with fresh reads and empty barriers."""
+    assert _violations(T, D, None, range(12)) == []
+
+
+@pytest.mark.parametrize("T", [3, 6, 13])
+def test_head_protocol_intake_failure_exits_every_role_at_the_same_step(T):
+    for fail_at in range(1, T):
+        assert _violations(T, 9, fail_at, range(8)) == [], fail_at
+
+
+@pytest.mark.parametrize("mutate", ["no_pair", "no_pre", "no_early_slot", "no_copy_wait"])
+def test_head_protocol_model_detects_a_missing_wait(mutate):
+    """The model has teeth: dropping any one wait of the protocol is caught."""
+    found = _violations(13, 20, None, range(12), mutate) + _violations(5, 3, None, range(12), mutate)
+    assert found
