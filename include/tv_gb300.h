@@ -117,6 +117,16 @@ int tv_model_set_path(tv_model m, int path, int grid_ctas);
  * TV_PATH_GRID). */
 int tv_model_last_path(tv_model m);
 
+/* Threads per CTA of the most recent batched decode on this model, 0 before
+ * any (no reference counterpart).  The batched decodes (tv_decode_batch,
+ * tv_decode_batch_device) take the CTA shape from an autotuner: the first
+ * batch of a (N, D) shape with at least two waves of CTAs times every
+ * candidate shape (128, 256, 384, 512 threads) on its own shortest
+ * sequences, waiting for those runs, and the fastest is kept for the
+ * process.  Setting the environment variable TV_AUTOTUNE=0 keeps the
+ * default shape (256).  Results never depend on the shape. */
+int tv_model_batch_threads(tv_model m);
+
 /* Kernel timing for benchmark reporting (no reference counterpart).  When
  * enabled, CUDA events on the decode's own stream bracket its main kernel;
  * tv_model_kernel_ms waits for that kernel and returns its time in ms for

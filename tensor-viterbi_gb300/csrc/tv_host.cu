@@ -14,8 +14,11 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -106,7 +109,27 @@ cudaError_t upload(void* dst, const void* src, size_t bytes) {
   return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
 }
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 256;  // one-CTA kernel: single decodes, the server, the static path
+
+// CTA shapes (threads per CTA) the batched decode chooses from.  The step
+// loop gives each warp whole states, so the best shape depends on N (warps
+// per state round), on D (the lanes' share of a state's window) and on how
+// many CTAs the window's shared memory lets an SM hold.
+constexpr int kCtaShapes[] = {128, 256, 384, 512};
+using CtaKernelFn = void (*)(tv::ModelView, tv::BatchView, tv::CtaLayout, unsigned char*);
+CtaKernelFn cta_kernel_for(int threads) {
+  switch (threads) {
+    case 128: return tv::cta_decode_kernel<128>;
+    case 384: return tv::cta_decode_kernel<384>;
+    case 512: return tv::cta_decode_kernel<512>;
+    default: return tv::cta_decode_kernel<256>;
+  }
+}
+
+// Autotuned CTA shape per (N, D, window in shared memory), measured once per
+// process on the first large batch of that shape.
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int>, int> g_tuned;
 
 // Log-space survival, accumulated from d = D-1 downwards with the running
 // two-term log-sum-exp of the reference (src/hsmm.cu:79-99); computed on the
@@ -153,8 +176,9 @@ struct tv_model_s {
   DevBuf<int> status;
   DevBuf<int> counter;
   DevBuf<int64_t> off;
-  DevBuf<int> order;
+  DevBuf<int> order, tune_order;
   DevBuf<unsigned char> scratch;
+  int batch_threads = 0;  // CTA shape of the last batched launch
   DevBuf<int32_t> obs_tmp, path_tmp;
   DevBuf<double> ll_tmp;
   int64_t last_launches = 0;
@@ -253,7 +277,7 @@ int check_obs_host(const int32_t* obs, int64_t T, int O) {
 // Launches the CTA-per-sequence kernel over n_seq sequences whose
 // observations / paths live on the device.  `off_host` has n_seq+1 entries.
 int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_t* obs_dev,
-                 int32_t* path_dev, double* ll_dev, cudaStream_t st) {
+                 int32_t* path_dev, double* ll_dev, cudaStream_t st, bool tune = false) {
   const int N = m->N, D = m->D;
   int64_t Tmax = 0;
   for (int k = 0; k < n_seq; ++k) {
@@ -293,24 +317,25 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
   TV_CUDA(cudaGetDevice(&dev));
   int smem_optin = 0;
   TV_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  auto kern = tv::cta_decode_kernel<kThreads>;
   size_t dyn = 0;
   const size_t static_smem = 64;
   if (L.bytes + static_smem <= (size_t)smem_optin) {
     L.in_smem = 1;
     dyn = L.bytes;
-    TV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
   }
-  int per_sm = 1;
-  TV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, dyn));
-  per_sm = std::max(per_sm, 1);
-  int grid = std::min(n_seq, m->sm_count * per_sm);
-  grid = std::max(grid, 1);
-  unsigned char* scratch = nullptr;
-  if (!L.in_smem) {
-    if ((rc = m->scratch.ensure((size_t)grid * L.bytes)) != TV_OK) return rc;
-    scratch = m->scratch.p;
-  }
+  // grid of a shape: as many CTAs as the SMs hold, at most one per sequence
+  auto prepare = [&](int threads, int n, int& grid) -> int {
+    const CtaKernelFn kern = cta_kernel_for(threads);
+    if (dyn) TV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    int per_sm = 1;
+    TV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, dyn));
+    grid = std::max(1, std::min(n, m->sm_count * std::max(per_sm, 1)));
+    if (!L.in_smem) {
+      int rc2;
+      if ((rc2 = m->scratch.ensure((size_t)grid * L.bytes)) != TV_OK) return rc2;
+    }
+    return TV_OK;
+  };
   tv::BatchView bv{};
   bv.obs = obs_dev;
   bv.off = m->off.p;
@@ -321,8 +346,73 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
   bv.next = m->counter.p;
   bv.order = order_dev;
   bv.n_seq = n_seq;
+
+  // The CTA shape: the tuned one for this (N, D, placement), else 256.  A
+  // batch of at least two waves of CTAs with no tuned shape yet measures
+  // every shape on its own shortest sequences (one wave) and keeps the
+  // fastest; TV_AUTOTUNE=0 turns this off.
+  int threads = kThreads;
+  const auto key = std::make_tuple(N, D, L.in_smem);
+  bool tuned = false;
+  if (tune) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      threads = it->second;
+      tuned = true;
+    }
+  }
+  const char* env = std::getenv("TV_AUTOTUNE");
+  const bool tune_on = !(env && env[0] == '0');
+  if (!tuned && tune_on && tune && n_seq >= 2 * m->sm_count) {
+    const int n_s = std::min(n_seq, m->sm_count * 2);
+    // the n_s shortest sequences, longest first, as the sample's order
+    std::vector<int> ord((size_t)n_seq);
+    for (int k = 0; k < n_seq; ++k) ord[k] = k;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+      return off_host[a + 1] - off_host[a] > off_host[b + 1] - off_host[b];
+    });
+    std::vector<int> sample(ord.end() - n_s, ord.end());
+    if ((rc = m->tune_order.ensure((size_t)n_s)) != TV_OK) return rc;
+    TV_CUDA(cudaMemcpyAsync(m->tune_order.p, sample.data(), sizeof(int) * n_s, cudaMemcpyHostToDevice, st));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    TV_CUDA(cudaEventCreate(&e0));
+    TV_CUDA(cudaEventCreate(&e1));
+    float best_ms = 0.0f;
+    int best = kThreads;
+    for (int shape : kCtaShapes) {
+      int grid = 1;
+      if ((rc = prepare(shape, n_s, grid)) != TV_OK) break;
+      tv::BatchView sv = bv;
+      sv.order = m->tune_order.p;
+      sv.n_seq = n_s;
+      TV_CUDA(cudaMemsetAsync(m->counter.p, 0, sizeof(int), st));
+      TV_CUDA(cudaEventRecord(e0, st));
+      cta_kernel_for(shape)<<<grid, shape, dyn, st>>>(view(m, Q), sv, L, L.in_smem ? nullptr : m->scratch.p);
+      TV_CUDA(cudaGetLastError());
+      TV_CUDA(cudaEventRecord(e1, st));
+      TV_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.0f;
+      TV_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      m->last_launches += 1;
+      if (shape == kCtaShapes[0] || ms < best_ms) {
+        best_ms = ms;
+        best = shape;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != TV_OK) return rc;
+    threads = best;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[key] = best;
+    TV_CUDA(cudaMemsetAsync(m->counter.p, 0, sizeof(int), st));
+  }
+  int grid = 1;
+  if ((rc = prepare(threads, n_seq, grid)) != TV_OK) return rc;
+  m->batch_threads = threads;
   mark_start(m, st);
-  kern<<<grid, kThreads, dyn, st>>>(view(m, Q), bv, L, scratch);
+  cta_kernel_for(threads)<<<grid, threads, dyn, st>>>(view(m, Q), bv, L, L.in_smem ? nullptr : m->scratch.p);
   TV_CUDA(cudaGetLastError());
   mark_end(m, st);
   m->last_launches += 1;
@@ -964,6 +1054,8 @@ int tv_model_set_path(tv_model m, int path, int grid_ctas) {
 
 int tv_model_last_path(tv_model m) { return m ? m->last_path : 0; }
 
+int tv_model_batch_threads(tv_model m) { return m ? m->batch_threads : 0; }
+
 int tv_model_set_timing(tv_model m, int enable) {
   if (!m) return fail(TV_EINVAL, "null model");
   std::lock_guard<std::mutex> lk(m->mu);
@@ -1021,7 +1113,7 @@ int tv_decode_batch_device(tv_model m, int n_seq, const int64_t* offsets, const 
   std::lock_guard<std::mutex> lk(m->mu);
   m->last_launches = 0;
   if (offsets[0] != 0) return fail(TV_EINVAL, "offsets[0] must be 0");
-  return launch_batch(m, n_seq, offsets, obs_dev, path_dev, ll_dev, (cudaStream_t)stream);
+  return launch_batch(m, n_seq, offsets, obs_dev, path_dev, ll_dev, (cudaStream_t)stream, true);
 }
 
 int tv_decode_batch(tv_model m, int n_seq, const int64_t* offsets, const int32_t* obs, int32_t* path,
@@ -1040,7 +1132,8 @@ int tv_decode_batch(tv_model m, int n_seq, const int64_t* offsets, const int32_t
   if ((rc = m->path_tmp.ensure((size_t)total)) != TV_OK) return rc;
   if ((rc = m->ll_tmp.ensure((size_t)n_seq)) != TV_OK) return rc;
   TV_CUDA(cudaMemcpyAsync(m->obs_tmp.p, obs, sizeof(int32_t) * total, cudaMemcpyHostToDevice, st));
-  if ((rc = launch_batch(m, n_seq, offsets, m->obs_tmp.p, m->path_tmp.p, m->ll_tmp.p, st)) != TV_OK) return rc;
+  if ((rc = launch_batch(m, n_seq, offsets, m->obs_tmp.p, m->path_tmp.p, m->ll_tmp.p, st, true)) != TV_OK)
+    return rc;
   TV_CUDA(cudaMemcpyAsync(path, m->path_tmp.p, sizeof(int32_t) * total, cudaMemcpyDeviceToHost, st));
   std::vector<double> ll((size_t)n_seq);
   TV_CUDA(cudaMemcpyAsync(ll.data(), m->ll_tmp.p, sizeof(double) * n_seq, cudaMemcpyDeviceToHost, st));

@@ -196,6 +196,11 @@ class Model:
         return {_lib.TV_PATH_CTA: "cta", _lib.TV_PATH_GRID: "grid"}.get(
             int(_lib.lib().tv_model_last_path(self._h)), "none")
 
+    def batch_threads(self) -> int:
+        """Threads per CTA of the most recent batched decode (the autotuned
+        shape), 0 before any."""
+        return int(_lib.lib().tv_model_batch_threads(self._h))
+
 
 class GaussianModel(Model):
     """A model whose emissions are Gaussian per state: the (T x N)

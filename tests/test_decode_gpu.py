@@ -67,6 +67,40 @@ def test_model_reuse_and_batch_equal_single(tvlib):
         assert l1 == ref["loglik"]
 
 
+def test_batch_autotuned_cta_shape(tvlib):
+    """A batch of two waves of CTAs or more tunes the CTA shape once per
+    (N, D) and decodes with it; every path equals the one-at-a-time decode,
+    and the oracle on a sample.  TV_AUTOTUNE=0 keeps the default shape."""
+    import os
+    import tensor_viterbi.synthetic as syn
+    prob, seqs = syn.batch_problem(n_seq=320, N=10, D=60, M=16, lo=60, hi=400, seed=21)
+    with tvlib.Model(*prob.model_args()) as m:
+        paths, lls = m.decode_batch(seqs, return_loglik=True)
+        shape = m.batch_threads()
+        assert shape in (128, 256, 384, 512)
+        paths2, lls2 = m.decode_batch(seqs, return_loglik=True)
+        assert m.batch_threads() == shape  # kept for the process
+        for k in range(0, len(seqs), 37):
+            p1, l1 = m.decode(seqs[k], return_loglik=True)
+            np.testing.assert_array_equal(paths[k], p1)
+            np.testing.assert_array_equal(paths2[k], p1)
+            assert lls[k] == l1 == lls2[k]
+            ref = orc.decode(*prob.model_args(), seqs[k])
+            np.testing.assert_array_equal(p1, ref["path"])
+            assert l1 == ref["loglik"]
+    prob2, seqs2 = syn.batch_problem(n_seq=320, N=10, D=70, M=16, lo=70, hi=300, seed=22)
+    os.environ["TV_AUTOTUNE"] = "0"
+    try:
+        with tvlib.Model(*prob2.model_args()) as m:
+            paths, lls = m.decode_batch(seqs2, return_loglik=True)
+            assert m.batch_threads() == 256
+            p1, l1 = m.decode(seqs2[5], return_loglik=True)
+            np.testing.assert_array_equal(paths[5], p1)
+            assert lls[5] == l1
+    finally:
+        del os.environ["TV_AUTOTUNE"]
+
+
 def test_errors_are_returned_not_fatal(tvlib):
     args, _ = load_golden("syn_config0")
     N, tm, em, dl, sp, dp, obs = args
