@@ -375,9 +375,16 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
     std::vector<int> sample(ord.end() - n_s, ord.end());
     if ((rc = m->tune_order.ensure((size_t)n_s)) != TV_OK) return rc;
     TV_CUDA(cudaMemcpyAsync(m->tune_order.p, sample.data(), sizeof(int) * n_s, cudaMemcpyHostToDevice, st));
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    TV_CUDA(cudaEventCreate(&e0));
-    TV_CUDA(cudaEventCreate(&e1));
+    struct Events {  // released on every return path
+      cudaEvent_t a = nullptr, b = nullptr;
+      ~Events() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+      }
+    } ev;
+    TV_CUDA(cudaEventCreate(&ev.a));
+    TV_CUDA(cudaEventCreate(&ev.b));
+    cudaEvent_t e0 = ev.a, e1 = ev.b;
     float best_ms = 0.0f;
     int best = kThreads;
     for (int shape : kCtaShapes) {
@@ -400,8 +407,6 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
         best = shape;
       }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     if (rc != TV_OK) return rc;
     threads = best;
     std::lock_guard<std::mutex> lk(g_tune_mu);
