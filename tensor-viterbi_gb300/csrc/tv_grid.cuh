@@ -297,8 +297,10 @@ __device__ __forceinline__ void send_partial(const GridBufs& B, const GridParams
 // ---------------------------------------------------------------------------
 // GW: the worker's window (slot scores, selected deltas, window sums, argmax
 // words) lives in a private global-memory buffer, served by L1/L2, and the
-// duration and transition rows are read from the model's tables; used when
-// N*D is too large for the workers' shared memory.
+// exact duration and transition rows are read from the model's tables; used
+// when N*D is too large for the workers' shared memory.  The fixed-point
+// duration rows, read every step by the scan, stay in shared memory when they
+// fit there (P.w_qd_smem).
 template <bool GW>
 __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridBufs& B, unsigned char* sm) {
   constexpr int L = GRID_L;
