@@ -783,13 +783,13 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
   //                         t-1 and then the dense phase of delta[t]
   //   [cs, cs+csb)          (when split) the upper half of each matvec, a warp
   //                         per 32 states, handed over through shared memory
-  //   [cs, cs+2*st)         state helpers in two groups, one lane per state;
+  //   [cs+csb, +2*st)       state helpers in two groups, one lane per state;
   //                         group g prepares step t+1 for the steps t of parity
   //                         g (certification and exact winner over d >= 1), then
   //                         stores step t-1's results and slot t-1's messages;
   //                         a group has two steps for its work, so its serial
   //                         chain overlaps the other's
-  //   [cs+2*st, nthr)       intake: the workers' partial winners (a lane takes
+  //   [cs+csb+2*st, nthr)   intake: the workers' partial winners (a lane takes
   //                         segments pk and pk + in), the emission prefix (one
   //                         lane per state), the window-sum copies and the coarse
   //                         base
