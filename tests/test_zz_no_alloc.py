@@ -67,3 +67,37 @@ def test_fixed_scratch_entry_rejects_oversized_problems(tvlib):
     with tvlib.Model(*prob.model_args()) as m:
         with pytest.raises(ValueError, match="scratch"):
             m.decode_device_static(obs.data_ptr(), T, out.data_ptr())
+
+
+def test_fixed_scratch_entry_replays_from_a_cuda_graph(tvlib):
+    """A serving loop's form: the decode captured once in a CUDA graph, then
+    replayed for new observations copied into the captured input buffer.
+    Every replay equals the allocating entry point on the same sequence."""
+    import torch
+    import tensor_viterbi.synthetic as syn
+
+    prob, seqs = syn.batch_problem(n_seq=4, N=8, D=90, M=12, lo=3000, hi=3001, seed=41)
+    T = min(s.size for s in seqs)
+    seqs = [np.ascontiguousarray(s[:T]) for s in seqs]
+    with tvlib.Model(*prob.model_args()) as m:
+        obs = torch.from_numpy(seqs[0]).cuda()
+        path = torch.full_like(obs, -1)
+        ll = torch.zeros(1, dtype=torch.float64, device="cuda")
+        status = torch.full((1,), 12345, dtype=torch.int32, device="cuda")
+        # one-time set-up of the fixed scratch, before any capture
+        m.decode_device_static(obs.data_ptr(), T, path.data_ptr(), ll.data_ptr(), status.data_ptr(),
+                               torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            m.decode_device_static(obs.data_ptr(), T, path.data_ptr(), ll.data_ptr(), status.data_ptr(),
+                                   torch.cuda.current_stream().cuda_stream)
+        for s in seqs[1:] + seqs[:1]:
+            obs.copy_(torch.from_numpy(s))
+            path.fill_(-1)
+            g.replay()
+            torch.cuda.synchronize()
+            ref_path, ref_ll = m.decode(s, return_loglik=True)
+            assert int(status.item()) == 0
+            np.testing.assert_array_equal(path.cpu().numpy(), ref_path)
+            assert float(ll.item()) == ref_ll
