@@ -1,4 +1,6 @@
-"""A CPU model of the grid head's step protocol (tv_grid.cuh, grid_head).
+"""CPU models of the grid kernel's step protocols (tv_grid.cuh): the head
+CTA (grid_head) and the worker pipeline (grid_worker, at the end of this
+file).
 
 The head CTA runs five roles that meet at named non-aligned barriers:
   * critical lanes: the matvec of slot t-1, then the dense phase of delta[t];
@@ -294,3 +296,153 @@ def test_head_protocol_model_detects_a_missing_wait(mutate):
     """The model has teeth: dropping any one wait of the protocol is caught."""
     found = _violations(13, 20, None, range(12), mutate) + _violations(5, 3, None, range(12), mutate)
     assert found
+
+
+# ---------------------------------------------------------------------------
+# Worker CTA (tv_grid.cuh, grid_worker): scan threads, a certify warp and an
+# intake warp meet at one CTA barrier per step (worker_sync_all) and a last
+# one after the loops.  During the scan of step t+1 the certify warp serves
+# step t (scan results by step parity, window sums E_t of three buffers) and
+# the intake warp loads the slot that enters the scan at step t+2.
+# ---------------------------------------------------------------------------
+
+def run_worker_protocol(T, D, fail_at, seed, mutate=None):
+    rnd = random.Random(seed)
+    bars, mem, errs, exits = {}, {}, [], {}
+    s_bad = [0, 0]
+    n_scan, n_serv = 4, 2
+    total = n_scan + n_serv
+
+    def bar(i):
+        return bars.setdefault(i, _Bar())
+
+    def W(key, ver):
+        mem[key] = ver
+
+    def R(who, key, ver):
+        if mem.get(key) != ver:
+            errs.append(f"{who}: read {key} holds step {mem.get(key)}, needs {ver}")
+
+    def sync(i, n, cnt):
+        b = bar(i)
+        g0 = b.gen
+        if b.expect is None:
+            b.expect = cnt
+        elif b.expect != cnt:
+            errs.append(f"barrier {i}: count {cnt} against {b.expect}")
+        b.count += n
+        if b.count >= b.expect:
+            b.count, b.expect, b.gen = 0, None, b.gen + 1
+        return ("wait", i, g0)
+
+    ALL = 2
+    # set-up: window sums of step 1 in buffer 1 (t % 3), slots below L loaded
+    # as they enter (none before step L+1 is scanned)
+    W(("acc", 1), 1)
+
+    def slot_ver(s):
+        return ("slot", s % D)
+
+    def scan(name, n):
+        for t in range(1, T):
+            tau = min(t, D)
+            # cells of d in [L, tau): slots t-1-d
+            for d in range(L, tau):
+                R(name, slot_ver(t - 1 - d), t - 1 - d)
+            R(name, ("acc", t % 3), t)
+            if t + 1 < T:
+                W(("acc", (t + 1) % 3), t + 1)
+            W(("red", t & 1), t)
+            yield sync(ALL, n, total)
+            if s_bad[(t - 1) & 1]:
+                exits[name] = t
+                break
+        yield sync(ALL, n, total)
+        yield ("done",)
+
+    def certify(name, n):
+        for t in range(1, T):
+            yield sync(ALL, n, total)
+            if s_bad[(t - 1) & 1]:
+                exits[name] = t
+                break
+            R(name, ("red", t & 1), t)
+            R(name, ("acc", t % 3), t)
+            tau = min(t, D)
+            for d in range(L, tau):
+                R(name, slot_ver(t - 1 - d), t - 1 - d)
+            if fail_at == t:
+                s_bad[t & 1] = 1
+        yield sync(ALL, n, total)
+        yield ("done",)
+
+    def intake(name, n):
+        for t in range(1, T):
+            yield sync(ALL, n, total)
+            if s_bad[(t - 1) & 1]:
+                exits[name] = t
+                break
+            # the slot that enters the scan at step t+2 (one step ahead of
+            # its first use, so the scan of step t+1 may run meanwhile)
+            sp = t + 1 - L if mutate != "late_slot" else t - L
+            if t + 2 < T and sp >= 0:
+                W(slot_ver(sp), sp)
+        yield sync(ALL, n, total)
+        yield ("done",)
+
+    actors = {"scan_a": scan("scan_a", n_scan // 2), "scan_b": scan("scan_b", n_scan // 2),
+              "certify": certify("certify", 1), "intake": intake("intake", 1)}
+    waiting = {k: None for k in actors}
+    done = set()
+    for _ in range(10 ** 6):
+        if len(done) == len(actors):
+            break
+        ready = [k for k in actors if k not in done and
+                 (waiting[k] is None or bars[waiting[k][1]].gen > waiting[k][2])]
+        if not ready:
+            raise _Deadlock(", ".join(k for k in actors if k not in done))
+        k = rnd.choice(ready)
+        waiting[k] = None
+        op = next(actors[k])
+        if op[0] == "wait":
+            waiting[k] = op
+        elif op[0] == "done":
+            done.add(k)
+    if fail_at is not None and fail_at + 1 < T:
+        left = {exits.get(k) for k in actors}
+        if len(left) != 1 or left.pop() != fail_at + 1:
+            errs.append(f"roles left at different steps: {exits}")
+    for i, b in bars.items():
+        if b.count:
+            errs.append(f"barrier {i} left with {b.count} arrivals")
+    return errs
+
+
+def _worker_violations(T, D, fail_at, seeds, mutate=None):
+    out = []
+    for seed in seeds:
+        try:
+            out += run_worker_protocol(T, D, fail_at, seed, mutate)
+        except _Deadlock as e:
+            out.append(f"deadlock: {e}")
+    return out
+
+
+@pytest.mark.parametrize("T", [1, 2, 9, 12, 30])
+@pytest.mark.parametrize("D", [9, 10, 16, 25])
+def test_worker_pipeline_runs_clean(T, D):
+    """Scan, certify and intake overlap without a stale read of the window
+    sums, the scan results or a slot, for any interleaving."""
+    assert _worker_violations(T, D, None, range(10)) == []
+
+
+@pytest.mark.parametrize("T", [6, 20])
+def test_worker_pipeline_failure_exits_every_role_at_the_same_step(T):
+    for fail_at in range(1, T - 1):
+        assert _worker_violations(T, 10, fail_at, range(6)) == [], fail_at
+
+
+def test_worker_pipeline_model_detects_a_slot_loaded_too_late():
+    """The model has teeth: an intake that loads, during the scan of step
+    t+1, the slot that scan already needs is caught as a stale read."""
+    assert _worker_violations(30, 12, None, range(10), mutate="late_slot")
