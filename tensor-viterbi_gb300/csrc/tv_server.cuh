@@ -62,6 +62,7 @@ size_t request_bytes(const SrvRequest& r, bool grid, int G) {
     b += 8 * T * tv::GRID_L * N;                           // window sums of the head's candidates
     b += 8 * D * ((D + tv::CK_STRIDE - 1) / tv::CK_STRIDE + 1) * N;  // checkpoints of the early window sums
     b += 8 * D * N;                                          // initialisation scores
+    b += 48 * D * N + 256 * (size_t)G;                       // worker windows when they are kept in L2
     b += 8 * ((size_t)tv::SLOT_RING * N * tv::SLOT_WORDS + (size_t)tv::PART_RING * (G + N) * tv::MSG_WORDS +
               (D + 2 * tv::GRID_L + 8) * N * 2);
   }
