@@ -127,6 +127,17 @@ int tv_model_last_path(tv_model m);
  * default shape (256).  Results never depend on the shape. */
 int tv_model_batch_threads(tv_model m);
 
+/* The whole-GPU grid kernel's plan for a shape, computed on the host alone
+ * (diagnostics and tests; no reference counterpart; no GPU needed).  For N
+ * states, D durations, G CTAs (the head and G-1 workers) and a per-CTA
+ * shared-memory limit, fills out[0..9] = {plan exists (1/0), threads per
+ * CTA, dynamic shared bytes per CTA, window in global memory (1/0), matvec
+ * split over two warps per 32 states (1/0), worker segments S, most
+ * segments of one worker, head threads with a role, fixed-point duration
+ * rows in shared memory with the window in global memory (1/0), workers
+ * that own cells}. */
+int tv_grid_plan_info(int N, int D, int G, int smem_optin, int force_l2, int64_t* out);
+
 /* Kernel timing for benchmark reporting (no reference counterpart).  When
  * enabled, CUDA events on the decode's own stream bracket its main kernel;
  * tv_model_kernel_ms waits for that kernel and returns its time in ms for

@@ -431,9 +431,9 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
 // its shared memory); otherwise the cells are cut into equal contiguous
 // chunks that may span several states.  A worker's intersection with a
 // state's row is a segment and yields one partial winner per step.
-bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridParams& P, std::vector<long long>& wr,
-               std::vector<int>& first, std::vector<int>& count, std::vector<int>& base) {
-  const int N = m->N, D = m->D, L = tv::GRID_L;
+bool plan_grid_nd(int N, int D, int G, int smem_optin, bool force_l2, tv::GridParams& P, std::vector<long long>& wr,
+                  std::vector<int>& first, std::vector<int>& count, std::vector<int>& base) {
+  const int L = tv::GRID_L;
   if (G < 2 || D <= L || N > tv::GRID_MAX_N || D > 65535) return false;
   const int Gw = G - 1;
   const long long ND = (long long)N * D;
@@ -616,6 +616,11 @@ bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridPara
   P.h_bytes = o;
   P.timeout = 1LL << 31;  // SM clock cycles, about a second: no legitimate wait comes close
   return std::max(P.w_bytes, P.h_bytes) + 256 <= (unsigned long long)smem_optin;
+}
+
+bool plan_grid(tv_model_s* m, int G, int smem_optin, bool force_l2, tv::GridParams& P, std::vector<long long>& wr,
+               std::vector<int>& first, std::vector<int>& count, std::vector<int>& base) {
+  return plan_grid_nd(m->N, m->D, G, smem_optin, force_l2, P, wr, first, count, base);
 }
 
 // The grid kernel instance for a plan: window in shared or global memory.
@@ -1060,6 +1065,29 @@ int tv_model_set_path(tv_model m, int path, int grid_ctas) {
 int tv_model_last_path(tv_model m) { return m ? m->last_path : 0; }
 
 int tv_model_batch_threads(tv_model m) { return m ? m->batch_threads : 0; }
+
+int tv_grid_plan_info(int N, int D, int G, int smem_optin, int force_l2, int64_t* out) {
+  if (!out) return fail(TV_EINVAL, "null argument");
+  for (int k = 0; k < 10; ++k) out[k] = 0;
+  if (N <= 0 || D <= 0 || G <= 0 || smem_optin <= 0) return fail(TV_EINVAL, "N, D, G and the shared-memory limit must be positive");
+  tv::GridParams P{};
+  std::vector<long long> wr;
+  std::vector<int> first, count, base;
+  if (!plan_grid_nd(N, D, G, smem_optin, force_l2 != 0, P, wr, first, count, base)) return TV_OK;
+  out[0] = 1;
+  out[1] = P.block;
+  out[2] = (int64_t)std::max(P.w_bytes, P.h_bytes);
+  out[3] = P.w_global;
+  out[4] = P.cs_split;
+  out[5] = P.S;
+  out[6] = P.max_seg;
+  out[7] = (int64_t)P.cs_threads * (1 + P.cs_split) + 2 * P.st_threads + P.in_threads;
+  out[8] = P.w_qd_smem;
+  int busy = 0;
+  for (int w = 0; w + 1 < G; ++w) busy += wr[2 * w] < wr[2 * w + 1] ? 1 : 0;
+  out[9] = busy;
+  return TV_OK;
+}
 
 int tv_model_set_timing(tv_model m, int enable) {
   if (!m) return fail(TV_EINVAL, "null model");

@@ -49,6 +49,7 @@ EXPORTS = {
     "tv_model_set_path": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "tv_model_last_path": (C.c_int, [C.c_void_p]),
     "tv_model_batch_threads": (C.c_int, [C.c_void_p]),
+    "tv_grid_plan_info": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     "tv_model_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "tv_model_kernel_ms": (C.c_double, [C.c_void_p]),
     "tv_decode_device_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
