@@ -439,6 +439,7 @@ bool plan_grid_nd(int N, int D, int G, int smem_optin, bool force_l2, tv::GridPa
   const long long ND = (long long)N * D;
   long long chunk = 0;
   int S = 0, max_seg = 0;
+  long long seg_cost = 0;  // cost of a worker's extra segment, in cells (0: equal chunks)
   auto partition = [&](bool row_aligned) {
     wr.assign(2 * (size_t)Gw, 0);
     const int k = Gw / N;
@@ -455,13 +456,52 @@ bool plan_grid_nd(int N, int D, int G, int smem_optin, bool force_l2, tv::GridPa
         }
       for (; w < Gw; ++w) wr[2 * w] = wr[2 * w + 1] = ND;
       chunk = part;
-    } else {
+    } else if (seg_cost <= 0) {
       chunk = (ND + Gw - 1) / Gw;
       for (int w = 0; w < Gw; ++w) {
         const long long lo = std::min((long long)w * chunk, ND), hi = std::min(lo + chunk, ND);
         wr[2 * w] = lo;
         wr[2 * w + 1] = hi;
       }
+    } else {
+      // Contiguous chunks of equal cost, a cell costing 1 and every segment
+      // after a worker's first costing seg_cost more (a second state's loop
+      // and reduction): the smallest per-worker cost C whose greedy cover
+      // needs at most Gw workers.
+      auto cover = [&](long long C, bool fill) -> int {
+        long long p = 0;
+        int w = 0;
+        while (p < ND) {
+          if (w == Gw) return Gw + 1;
+          const long long lo = p;
+          long long b = C;
+          for (;;) {
+            const long long end = (p / D + 1) * D;  // end of this state's row
+            const long long take = std::min(b, end - p);
+            p += take;
+            b -= take;
+            if (p == ND || p < end || b <= seg_cost) break;
+            b -= seg_cost;  // continue into the next state
+          }
+          if (fill) {
+            wr[2 * w] = lo;
+            wr[2 * w + 1] = p;
+          }
+          ++w;
+        }
+        if (fill)
+          for (int v = w; v < Gw; ++v) wr[2 * v] = wr[2 * v + 1] = ND;
+        return w;
+      };
+      long long lo = (ND + Gw - 1) / Gw, hi = ND;
+      while (lo < hi) {
+        const long long mid = (lo + hi) / 2;
+        if (cover(mid, false) <= Gw) hi = mid;
+        else lo = mid + 1;
+      }
+      cover(lo, true);
+      chunk = 0;
+      for (int w = 0; w < Gw; ++w) chunk = std::max(chunk, wr[2 * w + 1] - wr[2 * w]);
     }
     first.assign(N, 0);
     count.assign(N, 0);
@@ -520,6 +560,10 @@ bool plan_grid_nd(int N, int D, int G, int smem_optin, bool force_l2, tv::GridPa
     std::vector<int> f0 = first, c0 = count, b0 = base;
     const long long chunk0 = chunk;
     const int S0 = S, ms0 = max_seg;
+    // With the window in L2 a worker's second segment costs about a third of
+    // an equal share of the scan (its own loop start and reduction, measured
+    // at N=100 D=1e4), so such workers get fewer cells.
+    seg_cost = (ND + Gw - 1) / Gw / 3;
     partition(false);
     if (!head_roles_fit(S) || max_seg > 32) {
       wr = wr0; first = f0; count = c0; base = b0; chunk = chunk0; S = S0; max_seg = ms0;

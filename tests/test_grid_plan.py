@@ -68,10 +68,13 @@ def test_plan_of_the_default_bench_shape(tvlib):
 
 def test_plan_of_the_stress_shape(tvlib):
     """N=100 D=1e4 on 152 CTAs: the window goes to global memory, the
-    fixed-point duration rows stay in shared memory, every worker busy."""
+    fixed-point duration rows stay in shared memory; the chunks are of equal
+    cost, so workers that span two states hold fewer cells and a few CTAs
+    may stay idle."""
     p = plan(100, 10_000, 152)
     assert p["ok"] and p["l2"] == 1 and p["qd_smem"] == 1
-    assert p["max_seg"] == 2 and p["busy"] == 151
+    assert p["max_seg"] == 2 and 140 <= p["busy"] <= 151
+    assert p["S"] < 151 + 99                   # fewer chunks cross a state boundary than equal cuts would
     assert p["block"] == max(p["head"], WORKER_L2)
 
 
