@@ -250,7 +250,7 @@ struct tv_server_s {
           r->st = nullptr;
           r->ev = nullptr;
           --admitted;
-          // this one and the rest of this round go back in arrival order
+          // this one and the rest of this admission pass go back in arrival order
           for (size_t q2 = to_start.size(); q2-- > q + 1;) {
             SrvRequest* o = to_start[q2];
             in_use -= o->bytes;
