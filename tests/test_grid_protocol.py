@@ -1,6 +1,6 @@
 """CPU models of the grid kernel's step protocols (tv_grid.cuh): the head
-CTA (grid_head) and the worker pipeline (grid_worker, at the end of this
-file).
+CTA (grid_head), the worker pipeline (grid_worker) and the tagged message
+rings between them (further down this file).
 
 The head CTA runs five roles that meet at named non-aligned barriers:
   * critical lanes: the matvec of slot t-1, then the dense phase of delta[t];
@@ -446,3 +446,131 @@ def test_worker_pipeline_model_detects_a_slot_loaded_too_late():
     """The model has teeth: an intake that loads, during the scan of step
     t+1, the slot that scan already needs is caught as a stale read."""
     assert _worker_violations(30, 12, None, range(10), mutate="late_slot")
+
+
+# ---------------------------------------------------------------------------
+# Messages between the head and the workers (tv_grid.cuh): three tagged rings
+# in global memory, read by polling for the expected tag.
+#   partials   worker -> head, PART_RING rows: the worker's winners of step t
+#              (tag t), taken in by the head during its step t-1;
+#   slots      head -> workers, SLOT_RING rows: slot s (tag s+1), sent once the
+#              head has finished step s+1, taken in by a worker at iteration
+#              s+L-1 for its scan of step s+L+1;
+#   exact delta head -> workers, D + 2L + 8 rows: delta[s] (tag s+1), read by a
+#              worker's certification at step t for s in [t-D, t-1-L].
+# A poll that finds a newer tag than it waits for would wait until its time
+# limit: the model reports that as an overrun, and a writer that replaces a
+# partial the head has not taken in yet as lost.
+# ---------------------------------------------------------------------------
+
+PART_RING, SLOT_RING = 32, 64
+
+
+def run_message_protocol(T, D, n_workers, seed, part_ring=PART_RING, slot_ring=SLOT_RING, rd_extra=2 * L + 8):
+    rnd = random.Random(seed)
+    PART, SLOTS = part_ring, slot_ring
+    Rd = D + rd_extra
+    part = [[None] * PART for _ in range(n_workers)]   # tag per row, per worker
+    slot = [None] * SLOTS
+    dstar = [None] * Rd
+    errs = []
+    # set-up: delta[0] (tag 1)
+    dstar[0] = 1
+
+    def poll(ring, row, tag, who):
+        have = ring[row]
+        if have is not None and have > tag:
+            errs.append(f"{who}: row {row} already holds tag {have}, waited for {tag}")
+            return True   # do not block: the error is recorded
+        return have == tag
+
+    def head():
+        # set-up: the workers' partials of step 1 (no candidate d >= L yet)
+        if T > 1:
+            for w in range(n_workers):
+                while not poll(part[w], 1, 1, "head set-up"):
+                    yield
+                part[w][1] = -1
+        h = 1
+        while h < T:
+            # step h takes in every worker's partial of step h+1
+            if h + 1 < T:
+                for w in range(n_workers):
+                    while not poll(part[w], (h + 1) % PART, h + 1, "head"):
+                        yield
+                    part[w][(h + 1) % PART] = -(h + 1)   # taken in
+            # results of step h-1 (the helpers' stores after step h): slot h-1 and delta[h-1]
+            if h >= 2:
+                dstar[(h - 1) % Rd] = h
+            slot[(h - 1) % SLOTS] = h
+            h += 1
+            yield
+        # delta[T-2] is stored at the last step; the tail takes in step T's partials
+        for w in range(n_workers):
+            while not poll(part[w], T % PART, T, "head tail"):
+                yield
+
+    def worker(w):
+        for t in range(1, T):
+            tau = min(t, D)
+            # certification of step t (after the scan of step t): exact deltas
+            # of the candidates it may re-score
+            for d in range(L, tau):
+                s = t - 1 - d
+                while not poll(dstar, s % Rd, s + 1, f"worker {w} re-score"):
+                    yield
+            # send the partial of step t, if its row was taken in
+            row = t % PART
+            old = part[w][row]
+            if old is not None and old > 0:
+                errs.append(f"worker {w}: partial tag {old} lost to tag {t}")
+            part[w][row] = t
+            # intake: slot t+1-L for the scan of step t+2
+            sp = t + 1 - L
+            if t + 2 < T and sp >= 0:
+                while not poll(slot, sp % SLOTS, sp + 1, f"worker {w} slot"):
+                    yield
+            yield
+        # tail (t = T-1): exact deltas of every candidate, then the tail partial
+        t = T - 1
+        for d in range(L, min(t, D)):
+            s = t - 1 - d
+            while not poll(dstar, s % Rd, s + 1, f"worker {w} tail"):
+                yield
+        part[w][T % PART] = T
+
+    actors = {"head": head(), **{f"w{w}": worker(w) for w in range(n_workers)}}
+    live = dict(actors)
+    idle = 0
+    while live:
+        k = rnd.choice(list(live))
+        try:
+            next(live[k])
+        except StopIteration:
+            del live[k]
+        idle += 1
+        if idle > 200 * T * (n_workers + 1) * (D + 4):
+            errs.append("no progress: " + ", ".join(live))
+            break
+    return errs
+
+
+@pytest.mark.parametrize("T", [2, 9, 12, 40, 120])
+@pytest.mark.parametrize("D", [9, 12, 30])
+def test_message_rings_never_overrun(T, D):
+    """With the rings' sizes, no poll finds a newer tag than it waits for, no
+    partial is replaced before the head takes it in, and nobody waits for
+    ever, whatever the relative speeds of the head and the workers."""
+    for seed in range(6):
+        assert run_message_protocol(T, D, 3, seed) == [], seed
+
+
+@pytest.mark.parametrize("rings", [dict(part_ring=4), dict(slot_ring=4), dict(rd_extra=-2)])
+def test_message_model_detects_rings_that_are_too_small(rings):
+    """The model has teeth: a partial ring shorter than the workers' lead, a
+    slot ring shorter than the head's, or an exact-delta ring shorter than D
+    rows (the kernel keeps D + 2L + 8) is caught."""
+    found = []
+    for seed in range(12):
+        found += run_message_protocol(60, 12, 3, seed, **rings)
+    assert found
