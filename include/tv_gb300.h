@@ -156,9 +156,12 @@ double tv_model_kernel_ms(tv_model m);
  * Scratch (the fixed-point tables for this decode, the back-pointers and a
  * few control words) comes from one fixed array compiled into the library,
  * TV_STATIC_SCRATCH_BYTES large, that every GPU using the library holds until
- * the process exits.  Limits: 8*(O*N + N*N + N*D) + 4*T*N + 256 bytes must fit
- * in it, and the D-deep window must fit one CTA's shared memory
- * (34*N*D + 8*N*N bytes <= 227 KB); larger problems return TV_ETOOBIG.
+ * the process exits.  Limits: the scratch a decode needs,
+ *     r(8*O*N) + r(8*N*N) + r(8*N*D) + 256 + 4*T*N bytes,
+ * with r(x) = x rounded up to a multiple of 256 (three tables, the control
+ * words, the back-pointers), must fit in it, and the D-deep window must fit
+ * one CTA's shared memory (34*N*D + 8*N*N bytes <= 227 KB); larger problems
+ * return TV_ETOOBIG before anything is launched.
  *
  * The first call on a device looks the array up (cudaGetSymbolAddress) and
  * sets the kernel's shared-memory attribute with that device current; make

@@ -12,16 +12,21 @@
 #                                    arithmetic (-O2, OpenMP, no fast-math), the
 #                                    build the C restatement is pinned to
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
-# Exits 0 without building when the reference checkout or pybind11 is absent.
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+# The reference checkout is the argument, else $TV_REFERENCE_ROOT, else the
+# development host's read-only checkout at /root/reference.  The root found is
+# recorded in oracle/_ref/ROOT, where the tests and the fixture script look it
+# up.  Exits 0 without building when the checkout or pybind11 is absent.
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${TV_REFERENCE_ROOT:-/root/reference}}"
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 OUT="$HERE/_ref"
 if [[ ! -f "$REF/src/hsmm.cu" || ! -f "$REF/src/bindings.cpp" ]]; then
     echo "build_ref: reference sources not found under $REF; skipping" >&2
     exit 0
 fi
+mkdir -p "$OUT"
+echo "$REF" > "$OUT/ROOT"
 PY="${PYTHON:-python3}"
 if ! PYBIND_INC="$($PY -c 'import pybind11; print(pybind11.get_include())' 2>/dev/null)"; then
     echo "build_ref: pybind11 not importable; skipping" >&2

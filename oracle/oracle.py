@@ -124,6 +124,21 @@ def reference_module(kind: str = "ieee"):
     return mod
 
 
+def reference_root() -> pathlib.Path | None:
+    """The reference checkout: $TV_REFERENCE_ROOT, else the root that
+    oracle/build_ref.sh recorded when it compiled the reference here; None
+    when neither names an existing directory (the GPU host has no checkout)."""
+    env = os.environ.get("TV_REFERENCE_ROOT")
+    cands = [pathlib.Path(env)] if env else []
+    rec = HERE / "_ref" / "ROOT"
+    if rec.exists():
+        cands.append(pathlib.Path(rec.read_text().strip()))
+    for c in cands:
+        if (c / "src" / "hsmm.cu").exists():
+            return c
+    return None
+
+
 def cpu_count() -> int:
     try:
         return len(os.sched_getaffinity(0))

@@ -18,6 +18,8 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <set>
+#include <utility>
 #include <tuple>
 #include <string>
 #include <vector>
@@ -124,6 +126,29 @@ CtaKernelFn cta_kernel_for(int threads) {
     case 512: return tv::cta_decode_kernel<512>;
     default: return tv::cta_decode_kernel<256>;
   }
+}
+
+// Dynamic shared-memory limits.  A kernel that takes dynamic shared memory
+// gets the device's whole opt-in limit, less its own static shared memory,
+// once per device before its first launch there, and never a smaller value
+// afterwards.  The limit is process-wide state of the kernel: a value set per
+// call could be overwritten by another thread between its set and its launch,
+// and a launch needing more than the last value set would fail.
+std::mutex g_smem_mu;
+std::set<std::pair<int, const void*>> g_smem_done;
+
+int raise_smem_limit(const void* kern) {
+  int dev = 0;
+  TV_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_smem_mu);
+  if (g_smem_done.count({dev, kern})) return TV_OK;
+  int optin = 0;
+  TV_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa{};
+  TV_CUDA(cudaFuncGetAttributes(&fa, kern));
+  TV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  g_smem_done.insert({dev, kern});
+  return TV_OK;
 }
 
 // Autotuned CTA shape per (N, D, window in shared memory), measured once per
@@ -326,7 +351,10 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
   // grid of a shape: as many CTAs as the SMs hold, at most one per sequence
   auto prepare = [&](int threads, int n, int& grid) -> int {
     const CtaKernelFn kern = cta_kernel_for(threads);
-    if (dyn) TV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    if (dyn) {
+      const int rc2 = raise_smem_limit((const void*)kern);
+      if (rc2 != TV_OK) return rc2;
+    }
     int per_sm = 1;
     TV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, dyn));
     grid = std::max(1, std::min(n, m->sm_count * std::max(per_sm, 1)));
@@ -747,7 +775,7 @@ int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_
   void* args[] = {&mv, &Pc, &B};
   const size_t dyn = std::max(P.w_bytes, P.h_bytes);
   const void* kern = grid_kernel_for(P);
-  TV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  if ((rc = raise_smem_limit(kern)) != TV_OK) return rc;
   mark_start(m, st);
   TV_CUDA(cudaLaunchCooperativeKernel(kern, dim3(P.G), dim3(P.block), args, dyn, st));
   mark_end(m, st);
@@ -786,10 +814,10 @@ int launch_single(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* pat
       } else {
         const size_t dyn = std::max(P.w_bytes, P.h_bytes);
         const void* kern = grid_kernel_for(P);
-        TV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+        int rc;
+        if ((rc = raise_smem_limit(kern)) != TV_OK) return rc;
         TV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, P.block, dyn));
         if (per_sm < 1) return fail(TV_EINVAL, "grid kernel does not fit on an SM");
-        int rc;
         if ((rc = m->seg_first.ensure(first.size())) != TV_OK) return rc;
         if ((rc = m->seg_count.ensure(count.size())) != TV_OK) return rc;
         if ((rc = m->seg_base.ensure(base.size())) != TV_OK) return rc;
@@ -881,10 +909,8 @@ int static_scratch_for_current_device(unsigned char** out) {
     cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
     if (e != cudaSuccess || !p)
       return fail(TV_ECUDA, std::string("cudaGetSymbolAddress(static scratch): ") + cudaGetErrorString(e));
-    int smem_optin = 0;
-    TV_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    TV_CUDA(cudaFuncSetAttribute(tv::cta_decode_kernel<kThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 smem_optin - 64));
+    const int rc = raise_smem_limit((const void*)tv::cta_decode_kernel<kThreads>);
+    if (rc != TV_OK) return rc;
     g_static_ptr[dev] = (unsigned char*)p;
   }
   *out = g_static_ptr[dev];

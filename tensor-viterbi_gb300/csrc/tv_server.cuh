@@ -347,9 +347,8 @@ tv_server tv_server_create(int64_t budget_bytes, int max_inflight) {
     delete s;
     return nullptr;
   }
-  // the kernels' shared-memory limits, set once before any concurrent launch
-  cudaFuncSetAttribute(tv::cta_decode_kernel<kThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       s->smem_optin - 64);
+  // the one-CTA kernel's shared-memory limit, raised before any concurrent launch
+  raise_smem_limit((const void*)tv::cta_decode_kernel<kThreads>);
   s->th = std::thread([s] { s->loop(); });
   return s;
 }

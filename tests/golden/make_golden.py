@@ -28,10 +28,14 @@ import numpy as np
 
 HERE = pathlib.Path(__file__).resolve().parent
 REPO = HERE.parents[1]
-REF = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
-
 sys.path.insert(0, str(REPO))
 from oracle import oracle as orc  # noqa: E402
+
+# the checkout: the argument, else $TV_REFERENCE_ROOT or the root recorded by
+# oracle/build_ref.sh
+REF = pathlib.Path(sys.argv[1]) if len(sys.argv) > 1 else orc.reference_root()
+if REF is None:
+    sys.exit("make_golden: no reference checkout (pass its root or set TV_REFERENCE_ROOT)")
 
 spec = importlib.util.spec_from_file_location(
     "tv_synthetic", str(REPO / "tensor-viterbi_gb300" / "tensor_viterbi" / "synthetic.py"))

@@ -8,8 +8,10 @@ import numpy as np
 import pytest
 
 from conftest import load_golden
+from oracle import oracle as orc
 
-REF_DATA = pathlib.Path("/root/reference/data")
+_ROOT = orc.reference_root()
+REF_DATA = _ROOT / "data" if _ROOT else pathlib.Path("reference-checkout-absent")
 
 
 def _hsmm():

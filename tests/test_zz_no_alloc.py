@@ -101,3 +101,60 @@ def test_fixed_scratch_entry_replays_from_a_cuda_graph(tvlib):
             assert int(status.item()) == 0
             np.testing.assert_array_equal(path.cpu().numpy(), ref_path)
             assert float(ll.item()) == ref_ll
+
+
+def test_fixed_scratch_entry_after_allocating_decode_of_smaller_window(tvlib):
+    """The kernel's shared-memory limit is process-wide state.  After the
+    fixed-scratch set-up, an allocating decode of a model with a small window,
+    then a fixed-scratch decode of a model with a much larger window: the
+    second must still launch and equal the oracle."""
+    import torch
+    import tensor_viterbi.synthetic as syn
+    from oracle import oracle as orc
+
+    small = syn.discrete_problem(4, 20, 600, 6, 3.0, 12.0, seed=5)
+    big = syn.discrete_problem(30, 180, 900, 12, 10.0, 90.0, seed=6)  # 34*N*D + 8*N*N ~ 191 KB
+    stream = torch.cuda.current_stream().cuda_stream
+    with tvlib.Model(*big.model_args()) as mb, tvlib.Model(*small.model_args()) as ms:
+        obs_b = torch.from_numpy(big.obs_seq).cuda()
+        path_b = torch.full_like(obs_b, -1)
+        ll_b = torch.zeros(1, dtype=torch.float64, device="cuda")
+        mb.decode_device_static(obs_b.data_ptr(), obs_b.numel(), path_b.data_ptr(), ll_b.data_ptr(), 0, stream)
+        torch.cuda.synchronize()
+        ps, lls = ms.decode(small.obs_seq, return_loglik=True)  # small window through the allocating path
+        path_b.fill_(-1)
+        mb.decode_device_static(obs_b.data_ptr(), obs_b.numel(), path_b.data_ptr(), ll_b.data_ptr(), 0, stream)
+        torch.cuda.synchronize()
+        got_b, got_llb = path_b.cpu().numpy(), float(ll_b.item())
+    ref_s = orc.decode(*small.args())
+    ref_b = orc.decode(*big.args(), variant="omp")
+    np.testing.assert_array_equal(ps, ref_s["path"])
+    assert lls == ref_s["loglik"]
+    np.testing.assert_array_equal(got_b, ref_b["path"])
+    assert got_llb == ref_b["loglik"]
+
+
+def test_fixed_scratch_entry_size_limit_is_exact(tvlib):
+    """The scratch bound stated in the header, r(8ON) + r(8NN) + r(8ND) + 256
+    + 4TN with r() rounding up to 256 bytes: a problem that needs exactly the
+    whole array decodes (and equals the allocating entry point); one more
+    step is refused."""
+    import torch
+    import tensor_viterbi.synthetic as syn
+    from tensor_viterbi.viterbi import _lib
+
+    N, O, D = 10, 16, 100
+    r = lambda x: (x + 255) // 256 * 256
+    fixed = r(8 * O * N) + r(8 * N * N) + r(8 * N * D) + 256
+    T = (_lib.TV_STATIC_SCRATCH_BYTES - fixed) // (4 * N)
+    assert fixed + 4 * T * N == _lib.TV_STATIC_SCRATCH_BYTES  # this shape fills the array exactly
+    p = syn.discrete_problem(N, D, T + 1, O, 5.0, 50.0, seed=9)
+    with tvlib.Model(*p.model_args()) as m:
+        ref_path, ref_ll, path, ll, status = _decode_both(tvlib, m, np.ascontiguousarray(p.obs_seq[:T]))
+        obs = torch.from_numpy(p.obs_seq).cuda()
+        out = torch.empty_like(obs)
+        with pytest.raises(ValueError, match="scratch"):
+            m.decode_device_static(obs.data_ptr(), T + 1, out.data_ptr())
+    assert status == 0
+    np.testing.assert_array_equal(path, ref_path)
+    assert ll == ref_ll
