@@ -143,16 +143,47 @@ class ClockSampler:
                 "reasons": active, "samples": len(rows)}
 
 
-def cpu_sample(prob, w, threads: int, max_extra: int = 200):
-    """The oracle's OpenMP decoder on the T-prefix D + max_extra of the
-    workload.  Returns (cells/s, seconds, T_sample)."""
+def window_cells(Ts, N, D):
+    """Window cells the recursion evaluates over a T-prefix: N * min(t, D) at
+    every step t >= 1.  Over a whole sequence this is T*N*D less the ramp
+    (N*D^2/2), so a CPU rate taken with it is the steady-state rate of the
+    metric's cells."""
+    n = Ts - 1
+    ramp = min(n, D)
+    return N * (ramp * (ramp + 1) // 2 + max(0, n - D) * D)
+
+
+def prefix_for(w, cells_cap, longest):
+    """The longest T-prefix up to `longest` steps whose window cells stay
+    within cells_cap (at least D + 1000 steps, at most the workload's T)."""
+    N, D = w["N"], w["D"]
+    Ts = min(w["T"], longest)
+    while Ts > D + 1000 and window_cells(Ts, N, D) > cells_cap:
+        Ts -= max(1, (window_cells(Ts, N, D) - int(cells_cap)) // (N * D) + 1)
+    return max(min(w["T"], D + 1000), Ts)
+
+
+# CPU-baseline sample: the T-prefix 2D + 20000 (long enough for the window to
+# be fully rolled for 20000 steps), capped at ~1.1e10 window cells (about 30 s
+# of the host's cores); the reference arm's per-step sample is ~2e9 cells.
+CPU_BASELINE_CELLS = 1.1e10
+REFERENCE_STEP_CELLS = 2.0e9
+# Parity check of the timed workload: the IEEE oracle on the T-prefix 2D + 2000.
+PARITY_CELLS = 6.0e9
+
+
+def cpu_sample(prob, w, threads: int, cells_cap: float):
+    """The oracle's OpenMP decoder (-O3 -ffast-math build, the reference's CPU
+    flags) on a T-prefix of the workload.  Returns (cells/s, seconds,
+    T_sample, cells) with cells counted by window_cells."""
     from oracle import oracle as orc
-    Ts = min(w["T"], w["D"] + max_extra)
+    Ts = prefix_for(w, cells_cap, 2 * w["D"] + 20000)
     args = prob.model_args() + (prob.obs_seq[:Ts],)
     t0 = time.perf_counter()
     orc.decode(*args, variant="omp", nthreads=threads, fast=True)
     dt = time.perf_counter() - t0
-    return Ts * w["N"] * w["D"] / dt, dt, Ts
+    cells = window_cells(Ts, w["N"], w["D"])
+    return cells / dt, dt, Ts, cells
 
 
 def run_reference(args, w, wname):
@@ -164,15 +195,14 @@ def run_reference(args, w, wname):
     threads = orc.cpu_count()
     prob = make_problem(w)
     for _ in range(args.warmup):
-        cpu_sample(prob, w, threads)
-    vals, secs = [], []
+        cpu_sample(prob, w, threads, REFERENCE_STEP_CELLS)
+    secs = []
     for _ in range(args.steps):
-        v, dt, Ts = cpu_sample(prob, w, threads)
-        vals.append(v)
+        v, dt, Ts, cells = cpu_sample(prob, w, threads, REFERENCE_STEP_CELLS)
         secs.append(dt)
-    value = Ts * w["N"] * w["D"] * len(secs) / sum(secs)
-    sample = (f"T-prefix {Ts} of the workload ({Ts * w['N'] * w['D']:.3e} cells) per step, "
-              f"OpenMP restatement of src/hsmm.cu:376-600, {threads} threads")
+    value = cells * len(secs) / sum(secs)
+    sample = (f"T-prefix {Ts} of the workload per step ({cells:.3e} window cells, N*min(t,D) per step), "
+              f"OpenMP restatement of src/hsmm.cu:376-600 built -O3 -ffast-math, {threads} threads")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs),
@@ -282,10 +312,24 @@ def run_ours(args, w, wname):
             from oracle import oracle as orc
             orc.build()
             threads = orc.cpu_count()
-            v, dt, Ts = cpu_sample(prob, w, threads)
+            v, dt, Ts, cc = cpu_sample(prob, w, threads, CPU_BASELINE_CELLS)
             cpu = {"value": v, "unit": "cells/s", "cores": threads, "kind": "port",
-                   "sample": f"T-prefix {Ts} ({Ts * N * D:.3e} cells, {dt:.1f} s), OpenMP restatement of "
-                             f"src/hsmm.cu:376-600 built -O3 -ffast-math, {threads} threads"}
+                   "sample": f"T-prefix {Ts} ({cc:.3e} window cells, N*min(t,D) per step, {dt:.1f} s), "
+                             f"OpenMP restatement of src/hsmm.cu:376-600 built -O3 -ffast-math, {threads} threads"}
+        parity = None
+        if not args.no_parity:
+            # The timed workload's own model and observations, decoded on a
+            # T-prefix by the same model and kernel, against the IEEE oracle.
+            from oracle import oracle as orc
+            Tp = prefix_for(w, PARITY_CELLS, 2 * D + 2000)
+            obs_p = np.ascontiguousarray(prob.obs_seq[:Tp])
+            gp, gl = model.decode(obs_p, return_loglik=True)
+            t0 = time.perf_counter()
+            ref = orc.decode(*prob.model_args(), obs_p, variant="omp")
+            parity = {"T_prefix": Tp, "kernel_path": model.last_path(),
+                      "path_equal": bool(np.array_equal(gp, ref["path"])), "loglik_equal": gl == ref["loglik"],
+                      "oracle": "IEEE OpenMP restatement of src/hsmm.cu:376-600",
+                      "oracle_s": round(time.perf_counter() - t0, 1)}
         line = {
             "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -303,6 +347,7 @@ def run_ours(args, w, wname):
             "kernel_path": model.last_path(),
             "wall_s": wall,
             "consistent": same,
+            "parity": parity,
             "loglik": ll_host,
         }
         print(json.dumps(line), flush=True)
@@ -563,6 +608,21 @@ def run_batch(args, w, wname):
             cpu = {"value": cc / dt, "unit": "cells/s", "cores": threads, "kind": "port",
                    "sample": f"{cc / (N * D):.0f} steps of the mix decoded one sequence at a time ({dt:.1f} s), "
                              f"OpenMP restatement of src/hsmm.cu:376-600, {threads} threads"}
+        parity = None
+        if not args.no_parity:
+            # Sequences of the timed mix, as the batched launch decoded them,
+            # against the IEEE oracle: every 512th sequence of up to 2e4 steps.
+            from oracle import oracle as orc
+            pick = [k for k in range(0, len(my), 512) if my[k].size <= 20000][:8]
+            t0 = time.perf_counter()
+            ok_p = ok_l = True
+            for k in pick:
+                ref = orc.decode(*prob.model_args(), my[k], variant="omp")
+                ok_p = ok_p and bool(np.array_equal(paths[k], ref["path"]))
+                ok_l = ok_l and float(lls[k]) == ref["loglik"]
+            parity = {"sequences": len(pick), "path_equal": ok_p, "loglik_equal": ok_l,
+                      "oracle": "IEEE OpenMP restatement of src/hsmm.cu:376-600",
+                      "oracle_s": round(time.perf_counter() - t0, 1)}
         line = {
             "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -580,7 +640,7 @@ def run_batch(args, w, wname):
                     "ms_per_step": 1e3 * sum(e2e_s) / len(e2e_s)},
             "plain_loop": {"value": plain, "unit": "cells/s", "sample_sequences": int(len(samp)),
                            "speedup_batched_vs_plain": value / plain},
-            "gpu_launches": launches, "clocks": clk, "consistent": same,
+            "gpu_launches": launches, "clocks": clk, "consistent": same, "parity": parity,
         }
         print(json.dumps(line), flush=True)
     model.close()
@@ -624,6 +684,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="single_N75_D5000_T1e6")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of the workload's T-prefix")
     ap.add_argument("--no-e2e", action="store_true",
                     help="skip the host-buffer (drop-in call) measurement: long stress workloads")
     ap.add_argument("--T", type=int, default=0, help="override the sequence length (profiling runs)")

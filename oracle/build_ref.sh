@@ -4,13 +4,23 @@
 # from the read-only reference checkout into oracle/_ref/.  Nothing is copied
 # into this repository: the sources are compiled where they lie.
 #
-# Two builds are produced:
+# Three builds are produced:
 #   oracle/_ref/shipped/_native*.so  the reference's own CPU flags
 #                                    (CMakeLists.txt:131-136: -O3 -march=native
 #                                    -mtune=native -ffast-math, OpenMP)
 #   oracle/_ref/ieee/_native*.so     the same sources with plain IEEE
 #                                    arithmetic (-O2, OpenMP, no fast-math), the
 #                                    build the C restatement is pinned to
+#   oracle/_ref/cuda/kernels_sm103a.cubin
+#                                    the reference's CUDA kernels (src/kernels.cu)
+#                                    for sm_103a with its CUDA flags
+#                                    (CMakeLists.txt:141-148: -O3 -use_fast_math
+#                                    -Xptxas=-O3), plus kernels.names, their
+#                                    mangled names (nm of the host object).
+#                                    Device code only: it runs on the GPU host
+#                                    under oracle/ref_cuda.c, a host driver
+#                                    written here that restates the reference's
+#                                    launch sequence (src/hsmm.cu:604-791).
 #
 # Usage: oracle/build_ref.sh [REFERENCE_ROOT]
 # The reference checkout is the argument, else $TV_REFERENCE_ROOT, else the
@@ -50,6 +60,33 @@ build() {
     echo "build_ref: built $obj"
 }
 
+build_cuda() {
+    local out="$OUT/cuda"
+    local nv="${NVCC:-$(command -v nvcc || echo /usr/local/cuda/bin/nvcc)}"
+    if [[ ! -x "$nv" ]]; then
+        echo "build_ref: nvcc not found; the reference CUDA kernels are not built" >&2
+        return 0
+    fi
+    mkdir -p "$out"
+    if [[ -f "$out/kernels_sm103a.cubin" && "$out/kernels_sm103a.cubin" -nt "$REF/src/kernels.cu" \
+          && -f "$out/kernels.names" ]]; then
+        return 0
+    fi
+    local flags=(-gencode arch=compute_103a,code=sm_103a -O3 -use_fast_math -std=c++17 -I"$REF/src")
+    "$nv" -cubin "${flags[@]}" -Xptxas=-O3 "$REF/src/kernels.cu" -o "$out/kernels_sm103a.cubin.tmp"
+    "$nv" -c "${flags[@]}" "$REF/src/kernels.cu" -o "$out/kernels_host.o"
+    # "<name> <mangled>" per kernel; the name is the mangled name's
+    # length-prefixed identifier (_Z<len><name>...)
+    nm "$out/kernels_host.o" | awk '$2 == "T" && $3 ~ /^_Z[0-9]+kernel_/ {
+        s = substr($3, 3); match(s, /^[0-9]+/); len = substr(s, 1, RLENGTH) + 0;
+        print substr(s, RLENGTH + 1, len), $3 }' > "$out/kernels.names.tmp"
+    rm -f "$out/kernels_host.o"
+    mv "$out/kernels_sm103a.cubin.tmp" "$out/kernels_sm103a.cubin"
+    mv "$out/kernels.names.tmp" "$out/kernels.names"
+    echo "build_ref: built $out/kernels_sm103a.cubin"
+}
+
 build shipped -O3 -march=native -mtune=native -ffast-math &
 build ieee -O2 &
+build_cuda &
 wait

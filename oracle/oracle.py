@@ -51,6 +51,14 @@ def _load(name: str) -> C.CDLL:
         h.tvo_score_segments.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _ip, _ip, _bp]
         h.tvo_survival.restype = None
         h.tvo_survival.argtypes = [C.c_int, C.c_int, _dp, _dp]
+        if hasattr(h, "tvo_decode_cuda"):
+            h.tvo_decode_cuda.restype = C.c_int
+            h.tvo_decode_cuda.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _ip, C.c_int,
+                                          _dp, C.c_int, _ip, _dp, _dp]
+            h.tvo_lin_suffix.restype = None
+            h.tvo_lin_suffix.argtypes = [C.c_int, C.c_int, _dp, _dp]
+            h.tvo_block_scan.restype = None
+            h.tvo_block_scan.argtypes = [_dp, C.c_int, _dp]
         _libs[name] = h
         return h
 
@@ -122,6 +130,113 @@ def reference_module(kind: str = "ieee"):
     spec.loader.exec_module(mod)
     sys.modules[name] = mod
     return mod
+
+
+# Flag bits of decode_cuda_semantics: the reference CUDA backend's four
+# differences from its C++ decoder (tv_oracle_cuda.c).
+CU_INIT_SCAN, CU_WINDOW, CU_TAIL, CU_ITREE = 1, 2, 4, 8
+CU_ALL = 15
+CU_NAMES = {CU_INIT_SCAN: "init scan", CU_WINDOW: "window roll", CU_TAIL: "linear-survival tail",
+            CU_ITREE: "i-tree argmax"}
+
+
+def lin_suffix(n_states, duration_probs_linear):
+    """Linear duration suffix sums in kernel_initialization's block-scan
+    association, (N, D) [j][d]."""
+    h = _load("liboracle.so")
+    lin = _f64(duration_probs_linear)
+    D = lin.shape[0]
+    out = np.empty((int(n_states), D), dtype=np.float64)
+    h.tvo_lin_suffix(int(n_states), D, lin.ctypes.data_as(_dp), out.ctypes.data_as(_dp))
+    return out
+
+
+def block_scan(x):
+    """Inclusive prefix sums of x in kernel_initialization's association."""
+    h = _load("liboracle.so")
+    x = _f64(x).reshape(-1)
+    out = np.empty_like(x)
+    h.tvo_block_scan(x.ctypes.data_as(_dp), x.size, out.ctypes.data_as(_dp))
+    return out
+
+
+def decode_cuda_semantics(n_states, trans_mat, emission_probs, duration_probs_linear, start_probs,
+                          duration_probs, obs_seq, flags: int = CU_ALL, log_suffix=None, nthreads: int = 0):
+    """The reference CUDA backend's values with the differences in `flags`
+    (CU_* bits) and the C++ decoder's rules elsewhere (flags = 0 is the C++
+    decoder).  log_suffix (N, D) replaces the C library's log of lin_suffix()
+    in the tail (the device's log).  Returns dict(path, loglik, final)."""
+    h = _load("liboracle.so")
+    N = int(n_states)
+    tm, ep, lin = _f64(trans_mat), _f64(emission_probs), _f64(duration_probs_linear)
+    sp, dp = _f64(start_probs).reshape(-1), _f64(duration_probs)
+    obs = np.ascontiguousarray(np.asarray(obs_seq).astype(np.int32).reshape(-1))
+    O, D, T = ep.shape[0], dp.shape[0], obs.size
+    ls = None if log_suffix is None else _f64(log_suffix)
+    path = np.empty(T, dtype=np.int32)
+    ll = np.zeros(1, dtype=np.float64)
+    final = np.empty(N, dtype=np.float64)
+    rc = h.tvo_decode_cuda(N, O, D, T, tm.ctypes.data_as(_dp), ep.ctypes.data_as(_dp), lin.ctypes.data_as(_dp),
+                           sp.ctypes.data_as(_dp), dp.ctypes.data_as(_dp), obs.ctypes.data_as(_ip), int(flags),
+                           None if ls is None else ls.ctypes.data_as(_dp), int(nthreads),
+                           path.ctypes.data_as(_ip), ll.ctypes.data_as(_dp), final.ctypes.data_as(_dp))
+    if rc != 0:
+        raise ValueError(f"oracle: {STATUS.get(rc, rc)}")
+    return dict(path=path, loglik=float(ll[0]), final=final)
+
+
+def ref_cuda_files():
+    """(cubin, names) of the reference's CUDA kernels built by
+    oracle/build_ref.sh, or None when they are absent."""
+    d = HERE / "_ref" / "cuda"
+    cubin, names = d / "kernels_sm103a.cubin", d / "kernels.names"
+    return (cubin, names) if cubin.exists() and names.exists() else None
+
+
+_ref_cuda_lib = None
+
+
+def _ref_cuda():
+    global _ref_cuda_lib
+    with _lock:
+        if _ref_cuda_lib is None:
+            path = HERE / "libref_cuda.so"
+            if not path.exists():
+                build()
+            h = C.CDLL(str(path))
+            h.tvr_decode.restype = C.c_int
+            h.tvr_decode.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp,
+                                     _dp, _ip, _ip, _dp, _dp, _dp]
+            h.tvr_last_error.restype = C.c_char_p
+            _ref_cuda_lib = h
+    return _ref_cuda_lib
+
+
+def ref_cuda_decode(n_states, trans_mat, emission_probs, duration_probs_linear, start_probs, duration_probs,
+                    obs_seq):
+    """The reference's own CUDA kernels on this GPU (oracle/ref_cuda.c drives
+    them as src/hsmm.cu:604-791 does).  Returns dict(path, loglik, final,
+    ms_call, ms_kernels)."""
+    files = ref_cuda_files()
+    if files is None:
+        raise RuntimeError("the reference CUDA kernels are not built (oracle/build_ref.sh on a host with the checkout)")
+    h = _ref_cuda()
+    N = int(n_states)
+    tm, ep, lin = _f64(trans_mat), _f64(emission_probs), _f64(duration_probs_linear)
+    sp, dp = _f64(start_probs).reshape(-1), _f64(duration_probs)
+    obs = np.ascontiguousarray(np.asarray(obs_seq).astype(np.int32).reshape(-1))
+    O, D, T = ep.shape[0], dp.shape[0], obs.size
+    path = np.empty(T, dtype=np.int32)
+    ll = np.zeros(1, dtype=np.float64)
+    final = np.empty(N, dtype=np.float64)
+    ms = np.zeros(2, dtype=np.float64)
+    rc = h.tvr_decode(str(files[0]).encode(), str(files[1]).encode(), N, O, D, T, tm.ctypes.data_as(_dp),
+                      ep.ctypes.data_as(_dp), lin.ctypes.data_as(_dp), sp.ctypes.data_as(_dp),
+                      dp.ctypes.data_as(_dp), obs.ctypes.data_as(_ip), path.ctypes.data_as(_ip),
+                      ll.ctypes.data_as(_dp), final.ctypes.data_as(_dp), ms.ctypes.data_as(_dp))
+    if rc != 0:
+        raise RuntimeError(f"reference CUDA decode failed ({rc}): {h.tvr_last_error().decode()}")
+    return dict(path=path, loglik=float(ll[0]), final=final, ms_call=float(ms[0]), ms_kernels=float(ms[1]))
 
 
 def reference_root() -> pathlib.Path | None:

@@ -34,6 +34,16 @@ double tvo_score_segments(int N, int O, int D, int T,
                           const int32_t* obs, const int32_t* path,
                           const uint8_t* seg_start);
 
+/* tv_oracle_cuda.c: the reference CUDA backend's values (src/kernels.cu),
+ * each of its four differences from the C++ decoder switchable. */
+enum { TVO_CU_INIT_SCAN = 1, TVO_CU_WINDOW = 2, TVO_CU_TAIL = 4, TVO_CU_ITREE = 8, TVO_CU_ALL = 15 };
+void tvo_block_scan(const double* x, int n, double* out);
+void tvo_lin_suffix(int N, int D, const double* dur_lin, double* out);
+int tvo_decode_cuda(int N, int O, int D, int T, const double* trans, const double* emission,
+                    const double* dur_lin, const double* start, const double* duration,
+                    const int32_t* obs, int flags, const double* log_suffix, int nthreads,
+                    int32_t* path, double* loglik, double* final);
+
 #ifdef __cplusplus
 }
 #endif

@@ -44,3 +44,31 @@ def tvlib():
     from tensor_viterbi.viterbi import native
     native.configure("gb300", "cuda")
     return native
+
+
+# Oracle results at the benchmarked shapes, on T-prefixes long enough to reach
+# the fully rolled window (t > 2D): computed once per session and shared by the
+# parity tests of this decoder and of the reference's CUDA kernels.
+def _headline_prefix(prob):
+    Tp = 2 * prob.D + 2000
+    return prob.model_args() + (np.ascontiguousarray(prob.obs_seq[:Tp]),)
+
+
+@pytest.fixture(scope="session")
+def c1_case():
+    """N=75, D=5000, M=32: the single-sequence bench model (seed 1) and its
+    observations, T-prefix 2D + 2000 = 12000, with the oracle's result."""
+    import tensor_viterbi.synthetic as syn
+    from oracle import oracle as orc
+    args = _headline_prefix(syn.config1())
+    return args, orc.decode(*args, variant="omp")
+
+
+@pytest.fixture(scope="session")
+def c4_case():
+    """N=100, D=1e4, M=64: the stress-shape bench model (seed 4), T-prefix
+    2D + 2000 = 22000, with the oracle's result."""
+    import tensor_viterbi.synthetic as syn
+    from oracle import oracle as orc
+    args = _headline_prefix(syn.config4(T=1_000_000))
+    return args, orc.decode(*args, variant="omp")
