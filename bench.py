@@ -96,6 +96,25 @@ def committed_traffic(kernel: str, workload: str):
         return None
 
 
+def committed_onchip(kernel: str, workload: str, kernel_ms: float):
+    """L2 and shared-memory bytes per launch from a committed ncu summary
+    (profiles/traffic.json, scaled to the workload), as GB/s over the
+    measured kernel time."""
+    p = REPO / "profiles" / "traffic.json"
+    out = {"l2_gbs": None, "smem_gbs": None}
+    if not p.exists():
+        return out
+    try:
+        d = json.loads(p.read_text()).get(kernel + "_onchip", {}).get(workload)
+    except Exception:
+        return out
+    if d and kernel_ms and kernel_ms > 0:
+        out["l2_gbs"] = d["l2_bytes"] / (kernel_ms / 1e3) / 1e9
+        out["smem_gbs"] = d["smem_bytes"] / (kernel_ms / 1e3) / 1e9
+        out["onchip_source"] = d.get("source")
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -283,6 +302,11 @@ def run_ours(args, w, wname):
     kmean = statistics.mean(kern_ms) if kern_ms and min(kern_ms) > 0 else float("nan")
     achieved = ALGO_BYTES_PER_CELL * cells / (kmean / 1e3) / 1e9
     traffic = committed_traffic("grid_decode_kernel", wname)
+    # The recurrence is serial: the step period against the measured floor of
+    # the head's critical chain (matvec, exact score, barrier alone on one SM).
+    floor = None
+    if model.last_path() == "grid" and N <= 128:
+        floor = native.step_floor(N, D, 20000)
 
     # e2e: the drop-in call with host buffers, copies inside the timed region.
     h2d = (N * N + prob.O * N + N + 2 * D * N) * 8 + T * 4
@@ -338,7 +362,12 @@ def run_ours(args, w, wname):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "grid_decode_kernel", "kernel_ms": kmean,
-                         "algo_bytes_per_launch": ALGO_BYTES_PER_CELL * cells, "peak_source": peak_kind},
+                         "algo_bytes_per_launch": ALGO_BYTES_PER_CELL * cells, "peak_source": peak_kind,
+                         "step_us": 1e3 * kmean / T,
+                         "floor_us": floor["chain_us_per_step"] if floor else None,
+                         "step_over_floor": (1e3 * kmean / T) / floor["chain_us_per_step"] if floor else None,
+                         "xsm_roundtrip_us": floor["roundtrip_us"] if floor else None,
+                         **committed_onchip("grid_decode_kernel", wname, kmean)},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "cells/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": 1e3 * e2e_total / args.steps},

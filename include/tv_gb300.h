@@ -127,6 +127,16 @@ int tv_model_last_path(tv_model m);
  * default shape (256).  Results never depend on the shape. */
 int tv_model_batch_threads(tv_model m);
 
+/* Failure injection for tests (no reference counterpart; the reference's
+ * answer to any device failure is exit(EXIT_FAILURE), src/hsmm.cu:22-30).
+ * The next grid-kernel decode on this model loses one message: the worker
+ * partial of `step` for worker segment `segment` is never sent.  The head's
+ * bounded wait for it (or a worker's wait for the head, whichever gives up
+ * first) runs out after about a second of SM clocks; every CTA then leaves
+ * at the same step and the decode returns TV_ETIMEOUT, naming the wait.
+ * Applies to one decode; later decodes are unaffected. */
+int tv_model_drop_partial(tv_model m, int64_t step, int segment);
+
 /* The whole-GPU grid kernel's plan for a shape, computed on the host alone
  * (diagnostics and tests; no reference counterpart; no GPU needed).  For N
  * states, D durations, G CTAs (the head and G-1 workers) and a per-CTA
@@ -137,6 +147,17 @@ int tv_model_batch_threads(tv_model m);
  * rows in shared memory with the window in global memory (1/0), workers
  * that own cells}. */
 int tv_grid_plan_info(int N, int D, int G, int smem_optin, int force_l2, int64_t* out);
+
+/* Per-step latency floor of the grid decoder (diagnostics for benchmark
+ * reporting; no reference counterpart).  Runs, alone on one SM, the part of
+ * a step that only the head's critical lanes can do -- the packed N x N
+ * matvec with the grid plan's layout for (n_states, max_dur), the exact d = 0
+ * score, its fixed-point re-pack and the step barrier -- for `steps` steps,
+ * then bounces a tagged word between two SMs 2000 times.  out[0..6] = {clocks
+ * per step, microseconds per step (CUDA events), clocks per cross-SM round
+ * trip, microseconds per round trip, matvec split (1/0), SM ids of the two
+ * round-trip CTAs}.  Synchronous; allocates and frees its own buffers. */
+int tv_step_floor(int n_states, int max_dur, int64_t steps, double* out);
 
 /* Kernel timing for benchmark reporting (no reference counterpart).  When
  * enabled, CUDA events on the decode's own stream bracket its main kernel;

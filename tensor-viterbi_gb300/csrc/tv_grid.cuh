@@ -77,6 +77,12 @@ struct GridParams {
   int coarse_shift;   // fine-to-coarse right shift (f - COARSE_F)
   int coarse_margin;  // certified coarse i-margin, coarse units
   long long timeout;
+  long long copy_timeout;  // the head's wait for its own window-sum copies: fixed, so a copy is always drained
+  // Test-only fault injection (tv_model_drop_partial): the worker partial of
+  // step drop_tag for segment drop_seg is not sent, as if the message were
+  // lost; 0 = none (tags start at 1).
+  unsigned drop_tag;
+  int drop_seg;
 };
 
 struct GridBufs {
@@ -273,6 +279,7 @@ __device__ __forceinline__ ExactBest worker_reduce_exact(ExactBest eb, ExactBest
 
 __device__ __forceinline__ void send_partial(const GridBufs& B, const GridParams& P, unsigned tag, unsigned ring,
                                              int seg, const ExactBest& eb) {
+  if (tag == P.drop_tag && seg == P.drop_seg) return;  // test-only: a lost message
   TaggedMsg msg;
   const bool empty = eb.d == IDX_NONE;
   // the winner's order key and fixed-point value, and (d, i)
@@ -1261,7 +1268,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
       // the window sums of step t+2 (copied during the previous step) are in
       // before the group of step t+1 is released
       if (pk == 0 && t >= 2 && t + 2 < T) {
-        if (mbar_wait(&s_hwbar, (unsigned)(t & 1), P.timeout)) {
+        if (mbar_wait(&s_hwbar, (unsigned)(t & 1), P.copy_timeout)) {
           last_copy = -1;
         } else {
           grid_fail(B, TV_ETIMEOUT_DEV, SITE_HEAD_COPY);
@@ -1306,7 +1313,7 @@ __device__ void grid_head(const ModelView& m, const GridParams& P, const GridBuf
       }
     }
     // a copy still in flight after an early exit
-    if (pk == 0 && last_copy >= 0 && !mbar_wait(&s_hwbar, (unsigned)(last_copy & 1), P.timeout)) s_fb[0] = 1;
+    if (pk == 0 && last_copy >= 0 && !mbar_wait(&s_hwbar, (unsigned)(last_copy & 1), P.copy_timeout)) s_fb[0] = 1;
   }
   named_sync(BAR_END, nthr);
   if (s_fb[0] | s_fb[1]) return;

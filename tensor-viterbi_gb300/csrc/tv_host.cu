@@ -27,6 +27,7 @@
 #include "../../include/tv_gb300.h"
 #include "tv_cta.cuh"
 #include "tv_grid.cuh"
+#include "tv_floor.cuh"
 
 namespace {
 
@@ -217,6 +218,9 @@ struct tv_model_s {
   int plan_key_N = -1, plan_key_D = -1, plan_key_G = -1, plan_key_L2 = -1;
   tv::GridParams plan{};
   int path_pref = TV_PATH_AUTO, grid_ctas = 0, last_path = 0;
+  // test-only: a worker partial message the next grid decode drops
+  unsigned drop_tag = 0;
+  int drop_seg = -1;
   // optional events around the main kernel
   bool timing = false, timed = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -687,6 +691,9 @@ bool plan_grid_nd(int N, int D, int G, int smem_optin, bool force_l2, tv::GridPa
   if (P.qtr_smem) o += nn8;
   P.h_bytes = o;
   P.timeout = 1LL << 31;  // SM clock cycles, about a second: no legitimate wait comes close
+  P.copy_timeout = 1LL << 31;
+  P.drop_tag = 0;
+  P.drop_seg = -1;
   return std::max(P.w_bytes, P.h_bytes) + 256 <= (unsigned long long)smem_optin;
 }
 
@@ -772,6 +779,10 @@ int launch_grid(tv_model_s* m, const int32_t* obs_dev, int64_t T, int32_t* path_
     const double S_ = (double)T * (m->emax + m->tmax + m->dmax) + m->smax + (double)m->D * m->emax + m->tmax + m->dmax;
     Pc.coarse_margin = 4 + (int)std::ceil(2.0 * (q + 3.0 * u * S_) / qc) + 2;
   }
+  Pc.drop_tag = m->drop_tag;  // one decode only
+  Pc.drop_seg = m->drop_seg;
+  m->drop_tag = 0;
+  m->drop_seg = -1;
   void* args[] = {&mv, &Pc, &B};
   const size_t dyn = std::max(P.w_bytes, P.h_bytes);
   const void* kern = grid_kernel_for(P);
@@ -1136,6 +1147,13 @@ int tv_model_last_path(tv_model m) { return m ? m->last_path : 0; }
 
 int tv_model_batch_threads(tv_model m) { return m ? m->batch_threads : 0; }
 
+int tv_model_drop_partial(tv_model m, int64_t step, int segment) {
+  if (!m || step < 1 || step > 0xffffffffLL || segment < 0) return fail(TV_EINVAL, "bad argument");
+  m->drop_tag = (unsigned)step;
+  m->drop_seg = segment;
+  return TV_OK;
+}
+
 int tv_grid_plan_info(int N, int D, int G, int smem_optin, int force_l2, int64_t* out) {
   if (!out) return fail(TV_EINVAL, "null argument");
   for (int k = 0; k < 10; ++k) out[k] = 0;
@@ -1323,6 +1341,97 @@ int tv_decode_device_static(tv_model m, const int32_t* obs_dev, int64_t T, int32
   tv::cta_decode_kernel<kThreads><<<1, kThreads, L.bytes, st>>>(v, bv, L, nullptr);
   if (status_dev) static_status_kernel<<<1, 1, 0, st>>>(status, status_dev);
   TV_CUDA(cudaGetLastError());
+  return TV_OK;
+}
+
+int tv_step_floor(int n_states, int max_dur, int64_t steps, double* out) {
+  if (!out || n_states < 1 || n_states > tv::GRID_MAX_N || max_dur < 1 || steps < 1)
+    return fail(TV_EINVAL, "tv_step_floor: 1 <= n_states <= 128, max_dur >= 1, steps >= 1, out non-null");
+  int dev = 0, smem_optin = 0, sms = 0;
+  TV_CUDA(cudaGetDevice(&dev));
+  TV_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  TV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int N = n_states;
+  // the grid plan's own matvec layout for this shape (row padding, split)
+  tv::GridParams P;
+  std::vector<long long> wr;
+  std::vector<int> first, count, base;
+  int Np = (N + 15) / 16 * 16, split = 0;
+  if (plan_grid_nd(N, std::max(max_dur, 9), sms, smem_optin, false, P, wr, first, count, base)) {
+    Np = P.Np;
+    split = P.cs_split;
+  }
+  const int cs = (N + 31) / 32 * 32;
+  const int threads = cs * (split ? 2 : 1);
+  const size_t bytes = (size_t)4 * N * (Np + 4) + 8 * Np + 32 * N + 8 * (size_t)N * N + 12 * Np;
+  if (bytes > (size_t)smem_optin) return fail(TV_ETOOBIG, "tv_step_floor: tables exceed shared memory");
+  int rc;
+  if ((rc = raise_smem_limit((const void*)tv::floor_chain_kernel)) != TV_OK) return rc;
+  // transition scores of the benchmark family's range (log of Dirichlet rows)
+  std::vector<double> tr((size_t)N * N);
+  uint64_t x = 0x9e3779b97f4a7c15ull;
+  for (auto& v : tr) {
+    x ^= x << 13; x ^= x >> 7; x ^= x << 17;
+    v = std::log(1e-6 + (double)(x >> 11) * 0x1.0p-53);
+  }
+  struct Bufs {
+    double* tr = nullptr;
+    long long* out = nullptr;
+    unsigned long long* words = nullptr;
+    int* status = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ~Bufs() {
+      cudaFree(tr); cudaFree(out); cudaFree(words); cudaFree(status);
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+    }
+  } b;
+  TV_CUDA(cudaMalloc(&b.tr, sizeof(double) * tr.size()));
+  TV_CUDA(cudaMalloc(&b.out, sizeof(long long) * 8));
+  TV_CUDA(cudaMalloc(&b.words, sizeof(unsigned long long) * 4));
+  TV_CUDA(cudaMalloc(&b.status, sizeof(int)));
+  TV_CUDA(cudaMemcpy(b.tr, tr.data(), sizeof(double) * tr.size(), cudaMemcpyHostToDevice));
+  TV_CUDA(cudaMemset(b.out, 0, sizeof(long long) * 8));
+  TV_CUDA(cudaMemset(b.words, 0, sizeof(unsigned long long) * 4));
+  TV_CUDA(cudaMemset(b.status, 0, sizeof(int)));
+  TV_CUDA(cudaEventCreate(&b.e0));
+  TV_CUDA(cudaEventCreate(&b.e1));
+  const int f = 20;
+  const double scale = std::ldexp(1.0, f);
+  // warm-up, then the timed chain
+  tv::floor_chain_kernel<<<1, threads, bytes>>>(N, Np, split, std::min<int64_t>(steps, 1000), b.tr, scale,
+                                                f - tv::COARSE_F, b.out);
+  TV_CUDA(cudaGetLastError());
+  TV_CUDA(cudaEventRecord(b.e0));
+  tv::floor_chain_kernel<<<1, threads, bytes>>>(N, Np, split, steps, b.tr, scale, f - tv::COARSE_F, b.out);
+  TV_CUDA(cudaGetLastError());
+  TV_CUDA(cudaEventRecord(b.e1));
+  TV_CUDA(cudaEventSynchronize(b.e1));
+  long long hout[8] = {0};
+  TV_CUDA(cudaMemcpy(hout, b.out, sizeof(hout), cudaMemcpyDeviceToHost));
+  float ms = 0.0f;
+  TV_CUDA(cudaEventElapsedTime(&ms, b.e0, b.e1));
+  out[0] = (double)hout[0] / (double)steps;
+  out[1] = 1e3 * (double)ms / (double)steps;
+  // cross-SM round trip: one CTA per SM, CTA 0 and the last one
+  const size_t rt_smem = (size_t)smem_optin / 2 + 1024;
+  if ((rc = raise_smem_limit((const void*)tv::xsm_roundtrip_kernel)) != TV_OK) return rc;
+  const int iters = 2000;
+  long long limit = 1LL << 31;
+  void* args[] = {&b.words, (void*)&iters, &limit, &b.out, &b.status};
+  TV_CUDA(cudaMemset(b.out, 0, sizeof(long long) * 8));
+  TV_CUDA(cudaLaunchCooperativeKernel((const void*)tv::xsm_roundtrip_kernel, dim3(sms), dim3(32), args, rt_smem,
+                                      nullptr));
+  TV_CUDA(cudaDeviceSynchronize());
+  int st = 0;
+  TV_CUDA(cudaMemcpy(&st, b.status, sizeof(int), cudaMemcpyDeviceToHost));
+  TV_CUDA(cudaMemcpy(hout, b.out, sizeof(hout), cudaMemcpyDeviceToHost));
+  if (st != 0) return fail(TV_ETIMEOUT, "tv_step_floor: the cross-SM round trip timed out");
+  out[2] = (double)hout[0] / iters;
+  out[3] = out[2] * out[1] / std::max(out[0], 1e-9);
+  out[4] = (double)split;
+  out[5] = (double)hout[1];
+  out[6] = (double)hout[2];
   return TV_OK;
 }
 

@@ -49,9 +49,11 @@ EXPORTS = {
     "tv_model_set_path": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "tv_model_last_path": (C.c_int, [C.c_void_p]),
     "tv_model_batch_threads": (C.c_int, [C.c_void_p]),
+    "tv_model_drop_partial": (C.c_int, [C.c_void_p, C.c_int64, C.c_int]),
     "tv_grid_plan_info": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     "tv_model_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "tv_model_kernel_ms": (C.c_double, [C.c_void_p]),
+    "tv_step_floor": (C.c_int, [C.c_int, C.c_int, C.c_int64, _dp]),
     "tv_decode_device_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p]),
     "tv_gaussian_loglik": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, _dp, _dp, C.c_void_p, C.c_void_p]),

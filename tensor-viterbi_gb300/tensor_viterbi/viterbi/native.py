@@ -170,6 +170,12 @@ class Model:
             self._h, C.c_void_p(obs_dev_ptr), int(T), C.c_void_p(path_dev_ptr), C.c_void_p(loglik_dev_ptr or None),
             C.c_void_p(status_dev_ptr or None), C.c_void_p(stream or None)))
 
+    def drop_partial(self, step: int, segment: int = 0) -> None:
+        """Test-only failure injection: the next grid decode loses the worker
+        partial message of `step` for worker segment `segment`, and returns
+        TV_ETIMEOUT (RuntimeError) once the bounded wait for it runs out."""
+        _lib.check(_lib.lib().tv_model_drop_partial(self._h, int(step), int(segment)))
+
     def last_launches(self) -> int:
         return int(_lib.lib().tv_model_last_launches(self._h))
 
@@ -363,3 +369,14 @@ def decode_tensor_viterbi_omp(n_states, trans_mat, emission_probs, duration_prob
                               duration_probs, obs_seq) -> np.ndarray:
     _ensure_configured()
     raise RuntimeError("OMP backend not available in this build.")
+
+
+def step_floor(n_states: int, max_dur: int, steps: int = 20000) -> dict:
+    """Per-step latency floor of the grid decoder for a shape (diagnostics):
+    the head's critical chain alone on one SM, and one cross-SM tagged round
+    trip.  Returns clocks and microseconds per step and per round trip."""
+    out = np.zeros(7, dtype=np.float64)
+    _lib.check(_lib.lib().tv_step_floor(int(n_states), int(max_dur), int(steps), _lib.dptr(out)))
+    return {"chain_clocks_per_step": float(out[0]), "chain_us_per_step": float(out[1]),
+            "roundtrip_clocks": float(out[2]), "roundtrip_us": float(out[3]), "matvec_split": bool(out[4]),
+            "roundtrip_sms": [int(out[5]), int(out[6])]}

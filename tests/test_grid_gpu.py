@@ -177,3 +177,55 @@ def test_stress_shape_window_in_l2_properties(tvlib):
     sc = orc.score_segments(p.n_states, p.trans_mat, p.emission_probs, p.start_probs, p.duration_probs,
                             p.obs_seq, path, seg)
     assert abs(ll - sc) <= 1e-9 * abs(sc)
+
+
+def test_step_floor_probe(tvlib):
+    """The latency-floor probe of the head's critical chain and the cross-SM
+    round trip: both finish, report positive times, use the plan's matvec
+    split, and the chain alone is faster per step than a real decode."""
+    import tensor_viterbi.synthetic as syn
+    f = tvlib.step_floor(75, 5000, 5000)
+    assert f["chain_clocks_per_step"] > 0 and f["chain_us_per_step"] > 0
+    assert f["roundtrip_clocks"] > 0 and f["roundtrip_us"] > 0
+    assert f["roundtrip_sms"][0] != f["roundtrip_sms"][1]
+    import torch
+    from tensor_viterbi.viterbi import _lib
+    props = torch.cuda.get_device_properties(0)
+    optin = getattr(props, "shared_memory_per_block_optin", 232448)
+    info = np.zeros(10, dtype=np.int64)
+    _lib.check(_lib.lib().tv_grid_plan_info(75, 5000, props.multi_processor_count, optin, 0, info.ctypes.data))
+    assert f["matvec_split"] == bool(info[4])
+    p = syn.discrete_problem(75, 5000, 30000, 32, 50.0, 2500.0, seed=1)
+    with tvlib.Model(*p.model_args()) as m:
+        m.set_timing(True)
+        m.decode(p.obs_seq)
+        step_us = 1e3 * m.kernel_ms() / p.T
+    assert f["chain_us_per_step"] < step_us
+
+
+def test_lost_worker_message_times_out_and_the_next_decode_is_exact(tvlib):
+    """Failure handling of the grid kernel without a GPU fault: one worker
+    partial message is never sent (tv_model_drop_partial, the worker skips
+    that one store).  The bounded wait for it runs out after about a second
+    of SM clocks, every CTA leaves at the same step, and the decode returns
+    TV_ETIMEOUT naming the wait -- the reference exits the process on any
+    device failure (src/hsmm.cu:22-30).  The next decode on the same model
+    is exact."""
+    import time
+    import tensor_viterbi.synthetic as syn
+    p = syn.discrete_problem(20, 300, 3000, 16, 20.0, 150.0, seed=21)
+    ref = orc.decode(*p.args(), variant="omp")
+    with tvlib.Model(*p.model_args()) as m:
+        m.set_path("grid", 16)
+        m.drop_partial(1500, 0)
+        t0 = time.perf_counter()
+        with pytest.raises(RuntimeError, match="timed out") as ei:
+            m.decode(p.obs_seq)
+        waited = time.perf_counter() - t0
+        msg = str(ei.value)
+        assert "head waiting for worker partials" in msg or "worker waiting for a slot message" in msg, msg
+        assert 0.2 < waited < 30.0
+        path, ll = m.decode(p.obs_seq, return_loglik=True)
+        assert m.last_path() == "grid"
+    np.testing.assert_array_equal(path, ref["path"])
+    assert ll == ref["loglik"]
