@@ -54,9 +54,10 @@ WORKLOADS = {
     "batch_4096_N10_D250": dict(kind="batch", n_seq=4096, N=10, D=250, M=16, lo=1e3, hi=1e5, seed=2),
     # served: Poisson arrivals of requests with their own models; N from
     # {10,15,25,50}, D from {100,250,500,1000}, T log-uniform in [1e3, 1e6],
-    # half discrete (M = 32), half Gaussian; three arrival rates
-    "served_N10-50_D100-1000_T1e3-1e6": dict(kind="served", n_req=1000, Ns=[10, 15, 25, 50], Ds=[100, 250, 500, 1000],
-                                             Tlo=1e3, Thi=1e6, M=32, lo=5.0, hi=50.0, rates=[50.0, 200.0, 800.0],
+    # half discrete (M = 32), half Gaussian; arrival rates at fractions of the
+    # measured capacity
+    "served_N10-50_D100-1000_T1e3-1e6": dict(kind="served", n_req=5000, Ns=[10, 15, 25, 50], Ds=[100, 250, 500, 1000],
+                                             Tlo=1e3, Thi=1e6, M=32, lo=5.0, hi=50.0, loads=[0.25, 0.5, 0.8],
                                              seed=3),
 }
 
@@ -387,70 +388,75 @@ def run_ours(args, w, wname):
     return 0
 
 
-def served_requests(w):
-    """The served workload's requests: (kind, problem) with each request's own
-    seeded model; observations sampled from it."""
+def served_request(w, k):
+    """Request k of the served workload: (kind, problem, T), with its own
+    seeded model (seed (w.seed, k), so every arrival rate replays the same
+    requests) and observations sampled from it.  N from w.Ns, D from w.Ds, T
+    log-uniform in [Tlo, Thi]; odd requests Gaussian, even ones discrete."""
     import bisect
     import math
     import numpy as np
     import tensor_viterbi.synthetic as syn
-    rng = np.random.default_rng(w["seed"])
-    reqs = []
-    for k in range(w["n_req"]):
-        N = int(rng.choice(w["Ns"]))
-        D = int(rng.choice(w["Ds"]))
-        T = int(math.exp(rng.uniform(math.log(w["Tlo"]), math.log(w["Thi"]))))
-        T = max(T, D)
-        gauss = k % 2 == 1
-        lm = syn.random_model(rng, N, D, 2 if gauss else w["M"], w["lo"], w["hi"])
-        # segment-wise state path (bisect on cumulative rows: fast per segment)
-        cP = [list(np.cumsum(r) / r.sum()) for r in lm.P]
-        cA = [list(np.cumsum(r) / r.sum()) for r in lm.A]
-        cpi = list(np.cumsum(lm.pi) / lm.pi.sum())
-        u = rng.random(2 * T + 2).tolist()
-        states = np.empty(T, dtype=np.int32)
-        t, ui = 0, 0
-        s_ = min(bisect.bisect_right(cpi, u[ui]), N - 1)
-        ui += 1
-        while t < T:
-            dlen = min(bisect.bisect_right(cP[s_], u[ui]), D - 1) + 1
-            states[t:t + dlen] = s_
-            t += dlen
-            s_ = min(bisect.bisect_right(cA[s_], u[ui + 1]), N - 1)
-            ui += 2
-        if gauss:
-            mu = rng.normal(0.0, 2.0, size=N)
-            sd = rng.uniform(0.5, 2.0, size=N)
-            x = rng.normal(mu[states], sd[states])
-            p = syn.to_problem(lm, np.zeros(0, dtype=np.int32), emission_log=np.zeros((1, N)),
-                               meta=dict(x=x, mu=mu, sd=sd))
-            reqs.append(("gauss", p, T))
-        else:
-            obs = syn.sample_discrete_obs(rng, lm.B, states)
-            reqs.append(("disc", syn.to_problem(lm, obs), T))
-    return reqs
+    rng = np.random.default_rng([w["seed"], k])
+    N = int(rng.choice(w["Ns"]))
+    D = int(rng.choice(w["Ds"]))
+    T = max(int(math.exp(rng.uniform(math.log(w["Tlo"]), math.log(w["Thi"])))), D)
+    gauss = k % 2 == 1
+    lm = syn.random_model(rng, N, D, 2 if gauss else w["M"], w["lo"], w["hi"])
+    # segment-wise state path (bisect on cumulative rows: fast per segment)
+    cP = [list(np.cumsum(r) / r.sum()) for r in lm.P]
+    cA = [list(np.cumsum(r) / r.sum()) for r in lm.A]
+    cpi = list(np.cumsum(lm.pi) / lm.pi.sum())
+    u = rng.random(2 * T + 2).tolist()
+    states = np.empty(T, dtype=np.int32)
+    t, ui = 0, 0
+    s_ = min(bisect.bisect_right(cpi, u[ui]), N - 1)
+    ui += 1
+    while t < T:
+        dlen = min(bisect.bisect_right(cP[s_], u[ui]), D - 1) + 1
+        states[t:t + dlen] = s_
+        t += dlen
+        s_ = min(bisect.bisect_right(cA[s_], u[ui + 1]), N - 1)
+        ui += 2
+    if gauss:
+        mu = rng.normal(0.0, 2.0, size=N)
+        sd = rng.uniform(0.5, 2.0, size=N)
+        x = rng.normal(mu[states], sd[states])
+        p = syn.to_problem(lm, np.zeros(0, dtype=np.int32), emission_log=np.zeros((1, N)),
+                           meta=dict(x=x, mu=mu, sd=sd))
+        return "gauss", p, T
+    obs = syn.sample_discrete_obs(rng, lm.B, states)
+    return "disc", syn.to_problem(lm, obs), T
 
 
 def run_served(args, w, wname):
-    """Served decode: Poisson arrivals into the decode server at several
-    rates; latency from submission to completion (server clock), throughput
-    over the makespan; and the plain per-request loop on a sample."""
+    """Served decode.  First the saturated capacity: a burst of requests all
+    submitted at once, completed requests per second over the makespan.  Then
+    Poisson arrivals at fixed fractions of that capacity (--loads), the same
+    requests at every rate, generated just ahead of their arrival times.  Per
+    rate: p50/p99 of the whole latency (submission to completion), of the
+    service time (admission to completion) and of the queue time (submission
+    to admission), all on the server's clock; throughput over the makespan.
+    Beside it, the plain per-request loop on a sample of the same requests."""
+    import functools
+    import multiprocessing as mp
+    import queue as queue_mod
     import random
     import threading
     import numpy as np
+    # Requests are generated by a pool of host processes (spawned, before any
+    # CUDA work) so that generation keeps ahead of the highest arrival rate.
+    pool = mp.get_context("spawn").Pool(processes=max(1, min(8, (os.cpu_count() or 2) - 2)))
+    make = functools.partial(served_request, w)
     from tensor_viterbi.viterbi import native
     native.configure("gb300", "cuda")
-    reqs = served_requests(w)
-    cells = [T * p.n_states * p.D for _, p, T in reqs]
+    n_req = args.requests or w["n_req"]
 
     def submit(srv, kind, p):
         if kind == "disc":
             return srv.submit(*p.args())
         return srv.submit_gaussian(p.n_states, p.trans_mat, p.duration_probs_linear, p.start_probs,
                                    p.duration_probs, p.meta["x"], p.meta["mu"], p.meta["sd"])
-
-    # plain loop: the same kind of requests decoded one at a time (a sample)
-    sample = reqs[8:8 + 24]
 
     def plain(k, p):
         if k == "disc":
@@ -461,75 +467,100 @@ def run_served(args, w, wname):
                                       p.duration_probs, p.meta["x"], p.meta["mu"], p.meta["sd"]) as m:
                 m.decode()
 
-    plain(*reqs[0][:2])  # warm-up (context, kernel loading)
+    # plain loop: a sample of the same requests decoded one at a time
+    plain(*served_request(w, 0)[:2])  # warm-up (context, kernel loading)
+    sample = pool.map(make, range(8, 32))
     t0 = time.perf_counter()
     for k, p, _ in sample:
-        if k == "disc":
-            with native.Model(*p.model_args()) as m:
-                m.decode(p.obs_seq)
-        else:
-            with native.GaussianModel(p.n_states, p.trans_mat, p.duration_probs_linear, p.start_probs,
-                                      p.duration_probs, p.meta["x"], p.meta["mu"], p.meta["sd"]) as m:
-                m.decode()
+        plain(k, p)
     loop_rate = sum(T * p.n_states * p.D for _, p, T in sample) / (time.perf_counter() - t0)
-    # warm-up: a few requests through a server (kernel loading, pool growth)
-    with native.Server() as srv:
-        for t in [submit(srv, k, p) for k, p, _ in reqs[:8]]:
+    del sample
+    with native.Server() as srv:  # warm-up: kernel loading, pool growth
+        for t in [submit(srv, k, p) for k, p, _ in pool.map(make, range(8))]:
             srv.wait(t)
-    out = []
-    clocks = None
-    for rate in (w["rates"] if not args.rates else [float(r) for r in args.rates.split(",")]):
-        rnd = random.Random(int(rate) * 7919 + w["seed"])
+
+    def run_rate(n, rate):
+        """n requests; Poisson arrivals at `rate` per second, or all at once
+        when rate is None.  The process pool generates requests ahead of
+        their arrival (at most 64 waiting), a feeder thread submits them on
+        time, and this thread collects the results in submission order."""
+        rnd = random.Random(int((rate or 0) * 1000) * 7919 + w["seed"])
         arrivals, acc = [], 0.0
-        for _ in reqs:
-            acc += rnd.expovariate(rate)
+        for _ in range(n):
+            if rate:
+                acc += rnd.expovariate(rate)
             arrivals.append(acc)
+        made = queue_mod.Queue(maxsize=64)
+        tickets = [None] * n
+        cells = [0] * n
+        lat, svc, que, errors = [], [], [], []
+
+        def producer():
+            for item in pool.imap(make, range(n), chunksize=2):
+                made.put(item)
+
         with native.Server() as srv:
-            tickets = [None] * len(reqs)
+            prod = threading.Thread(target=producer, daemon=True)
+            prod.start()
+            ready = [made.get() for _ in range(n)] if rate is None else []  # a burst: all made first
             t0 = time.perf_counter()
 
             def feeder():
-                for i, (k, p, _) in enumerate(reqs):
+                for i in range(n):
+                    k, p, T = ready[i] if i < len(ready) else made.get()
                     dt = arrivals[i] - (time.perf_counter() - t0)
                     if dt > 0:
                         time.sleep(dt)
+                    cells[i] = T * p.n_states * p.D
                     tickets[i] = submit(srv, k, p)
 
             th = threading.Thread(target=feeder)
-            if clocks is None:
-                import torch
-                clocks = ClockSampler(torch.cuda.current_device())
-                clocks.start()
             th.start()
-            lat, queue, errors = [], [], []
-            for i in range(len(reqs)):
+            for i in range(n):
                 while tickets[i] is None:
                     time.sleep(0.0005)
                 try:
                     _, _, l_ms, q_ms = srv.wait(tickets[i])
                 except RuntimeError as e:
-                    k, p, T = reqs[i]
-                    errors.append(f"{k} N={p.n_states} D={p.D} T={T}: {e} stats={srv.stats()}")
+                    errors.append(f"request {i}: {e} stats={srv.stats()}")
                     continue
                 lat.append(l_ms)
-                queue.append(q_ms)
+                que.append(q_ms)
+                svc.append(l_ms - q_ms)
             th.join()
             makespan = time.perf_counter() - t0
             st = srv.stats()
-        out.append({"rate_per_s": rate, "requests": len(reqs), "p50_ms": float(np.percentile(lat, 50)),
-                    "p99_ms": float(np.percentile(lat, 99)), "mean_queue_ms": float(np.mean(queue)),
-                    "throughput_cells_per_s": sum(cells) / makespan, "makespan_s": makespan,
-                    "completed": st["completed"], "failed": st["failed"], "peak_bytes": st["peak_bytes"],
-                    "budget_bytes": st["budget"], "errors": errors[:3]})
-    clk = clocks.stop() if clocks else None
-    best = max(r["throughput_cells_per_s"] for r in out)
-    line = {"metric": "served decode: p50/p99 latency and cells/s at Poisson arrival rates", "value": best,
-            "unit": "cells/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": wname, "requests_per_rate": len(reqs), "N": w["Ns"], "D": w["Ds"],
-                       "T": f"log-uniform [{w['Tlo']:g}, {w['Thi']:g}]", "emissions": "half discrete (M=32), half Gaussian",
-                       "form": "served (continuous batching)"},
-            "rates": out, "plain_loop_cells_per_s": loop_rate, "vs_plain_loop": best / loop_rate,
-            "clocks": clk}
+        pct = lambda a, q: float(np.percentile(a, q)) if a else None
+        return {"requests": n, "completed": st["completed"], "failed": st["failed"],
+                "latency_p50_ms": pct(lat, 50), "latency_p99_ms": pct(lat, 99),
+                "service_p50_ms": pct(svc, 50), "service_p99_ms": pct(svc, 99),
+                "queue_p50_ms": pct(que, 50), "queue_p99_ms": pct(que, 99),
+                "throughput_cells_per_s": sum(cells) / makespan, "requests_per_s": len(lat) / makespan,
+                "makespan_s": makespan, "mean_cells_per_request": sum(cells) / n,
+                "peak_bytes": st["peak_bytes"], "budget_bytes": st["budget"], "errors": errors[:3]}
+
+    import torch
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    n_cap = min(n_req, args.capacity_requests)
+    cap = run_rate(n_cap, None)
+    capacity = cap["requests_per_s"]
+    out = []
+    loads = [float(x) for x in args.loads.split(",")] if args.loads else w["loads"]
+    for f in loads:
+        r = run_rate(n_req, f * capacity)
+        r.update({"offered_load": f, "rate_per_s": f * capacity})
+        out.append(r)
+    clk = clocks.stop()
+    pool.close()
+    line = {"metric": "served decode: p50/p99 latency (service and queue) and cells/s at fractions of capacity",
+            "value": cap["throughput_cells_per_s"], "unit": "cells/s", "n_gpus": 1, "higher_is_better": True,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wname, "requests_per_rate": n_req, "capacity_burst": n_cap, "N": w["Ns"],
+                       "D": w["Ds"], "T": f"log-uniform [{w['Tlo']:g}, {w['Thi']:g}]",
+                       "emissions": "half discrete (M=32), half Gaussian", "form": "served (continuous batching)"},
+            "capacity": cap, "rates": out, "plain_loop_cells_per_s": loop_rate,
+            "vs_plain_loop": cap["throughput_cells_per_s"] / loop_rate, "clocks": clk}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -717,8 +748,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true",
                     help="skip the host-buffer (drop-in call) measurement: long stress workloads")
     ap.add_argument("--T", type=int, default=0, help="override the sequence length (profiling runs)")
-    ap.add_argument("--rates", default="", help="served workload: comma-separated arrival rates (per s)")
+    ap.add_argument("--loads", default="", help="served workload: comma-separated fractions of the capacity")
     ap.add_argument("--requests", type=int, default=0, help="served workload: number of requests per rate")
+    ap.add_argument("--capacity-requests", type=int, default=1000,
+                    help="served workload: requests in the burst that measures the capacity")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload])
     if args.T:
