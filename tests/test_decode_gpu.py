@@ -112,3 +112,23 @@ def test_errors_are_returned_not_fatal(tvlib):
         tvlib.decode_tensor_viterbi_cuda(N, tm, em, dl, sp, dp, bad)
     # the library stays usable after an error
     np.testing.assert_array_equal(tvlib.decode_tensor_viterbi_cuda(*args), orc.decode(*args)["path"])
+
+
+@pytest.mark.parametrize("N,D,T", [(150, 400, 1000), (200, 64, 700)])
+def test_large_n_falls_back_to_one_cta_with_its_window_in_global_memory(tvlib, N, D, T):
+    """N above the grid kernel's 128 states, with a window far larger than one
+    CTA's shared memory (34*N*D + 8*N*N bytes: 2.2 MB and 0.75 MB): the
+    automatic choice is the one-CTA kernel with its window in global scratch,
+    which the reference's N (any N its reduction block takes) needs.  Exact
+    against the oracle; a forced grid is refused with a clear error."""
+    import tensor_viterbi.synthetic as syn
+    p = syn.discrete_problem(N, D, T, 24, 5.0, max(6.0, D / 2), seed=N + D)
+    ref = orc.decode(*p.args(), variant="omp")
+    with tvlib.Model(*p.model_args()) as m:
+        path, ll = m.decode(p.obs_seq, return_loglik=True)
+        assert m.last_path() == "cta"
+        m.set_path("grid")
+        with pytest.raises(ValueError, match="grid kernel cannot take this shape"):
+            m.decode(p.obs_seq)
+    np.testing.assert_array_equal(path, ref["path"])
+    assert ll == ref["loglik"]
