@@ -396,10 +396,10 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
         if (t + 4 < T) ob_pf = B.obs[t + 4];
       }
 
-      // Phase 1: the exact window folds of step t+1 into the next buffer
-      // (src/hsmm.cu:298-310): E_{t+1}[d] = E_t[d-1] + em_{t+1},
-      // E_{t+1}[0] = 0 + em_{t+1}; then the fixed-point scan over d in
-      // [L, tau).
+      // Phase 1: fixed-point scan over d in [L, tau), fused with the exact
+      // window folds of step t+1 into the next buffer (src/hsmm.cu:298-310):
+      // E_{t+1}[d] = E_t[d-1] + em_{t+1}, E_{t+1}[0] = 0 + em_{t+1}.  The FP64
+      // adds overlap the integer scan.
       const bool fold = (t1 < T) && (t1 > D + 1);
       Top2* redb = red + (int)(t & 1) * P.max_seg * NW;
       for (int s = 0; s < nseg; ++s) {
@@ -410,22 +410,6 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
         const double* ac = accb + a3 * accs + s * D - off0;
         double* an = accb + an3 * accs + s * D - off0;
         const double em1 = fold ? emw[(int)(t1 & 1) * P.max_seg + s] : 0.0;
-        // The exact window folds first, in a loop of their own: four
-        // independent loads and FP64 adds in flight per thread keep the FP64
-        // pipe busy (one warp-wide FP64 add per 64 clocks per sub-partition
-        // on GB300); the integer scan below then runs on the other pipes.
-        if (fold) {
-          int r = rb + tid;
-#pragma unroll 1
-          for (; r + 3 * WT < re; r += 4 * WT) {
-            const double x0 = ac[r], x1 = ac[r + WT], x2 = ac[r + 2 * WT], x3 = ac[r + 3 * WT];
-            an[r] = ((r == r0n) ? 0.0 : x0) + em1;
-            an[r + WT] = ((r + WT == r0n) ? 0.0 : x1) + em1;
-            an[r + 2 * WT] = ((r + 2 * WT == r0n) ? 0.0 : x2) + em1;
-            an[r + 3 * WT] = ((r + 3 * WT == r0n) ? 0.0 : x3) + em1;
-          }
-          for (; r < re; r += WT) an[r] = ((r == r0n) ? 0.0 : ac[r]) + em1;
-        }
         Top2 tb, tc;  // two independent chains, merged after the loop
         tb.init();
         tc.init();
@@ -441,11 +425,16 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
             const long long v0 = ct[r] + q[d], v1 = ct[r + WT] + q[d2];
             tb.push(v0, d);
             tc.push(v1, d2);
+            if (fold) {
+              an[r] = ((r == r0n) ? 0.0 : ac[r]) + em1;
+              an[r + WT] = ((r + WT == r0n) ? 0.0 : ac[r + WT]) + em1;
+            }
           }
           if (r < re) {
             int d = r0 - r;
             if (d < 0) d += D;
             tb.push(ct[r] + q[d], d);
+            if (fold) an[r] = ((r == r0n) ? 0.0 : ac[r]) + em1;
           }
         } else {
 #pragma unroll 4
@@ -453,6 +442,7 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
             int d = r0 - r;
             if (d < 0) d += D;
             if (d >= L && d < tau) tb.push(ct[r] + q[d], d);
+            if (fold) an[r] = ((r == r0n) ? 0.0 : ac[r]) + em1;
           }
         }
         tb.merge(tc.b1, tc.x1, tc.b2);
