@@ -410,40 +410,13 @@ __device__ void grid_worker(const ModelView& m, const GridParams& P, const GridB
         const double* ac = accb + a3 * accs + s * D - off0;
         double* an = accb + an3 * accs + s * D - off0;
         const double em1 = fold ? emw[(int)(t1 & 1) * P.max_seg + s] : 0.0;
-        Top2 tb, tc;  // independent chains, merged after the loop
+        Top2 tb, tc;  // two independent chains, merged after the loop
         tb.init();
         tc.init();
         if (qd_in_smem && tau == D) {
           // every d < D is in range; d < L is masked in the table
           int r = rb + tid;
-          Top2 te, tf;
-          te.init();
-          tf.init();
-#pragma unroll 1
-          for (; r + 3 * WT < re; r += 4 * WT) {
-            int d = r0 - r;
-            if (d < 0) d += D;
-            int d2 = d - WT;
-            if (d2 < 0) d2 += D;
-            int d3 = d2 - WT;
-            if (d3 < 0) d3 += D;
-            int d4 = d3 - WT;
-            if (d4 < 0) d4 += D;
-            const long long v0 = ct[r] + q[d], v1 = ct[r + WT] + q[d2];
-            const long long v2 = ct[r + 2 * WT] + q[d3], v3 = ct[r + 3 * WT] + q[d4];
-            tb.push(v0, d);
-            tc.push(v1, d2);
-            te.push(v2, d3);
-            tf.push(v3, d4);
-            if (fold) {
-              an[r] = ((r == r0n) ? 0.0 : ac[r]) + em1;
-              an[r + WT] = ((r + WT == r0n) ? 0.0 : ac[r + WT]) + em1;
-              an[r + 2 * WT] = ((r + 2 * WT == r0n) ? 0.0 : ac[r + 2 * WT]) + em1;
-              an[r + 3 * WT] = ((r + 3 * WT == r0n) ? 0.0 : ac[r + 3 * WT]) + em1;
-            }
-          }
-          tb.merge(te.b1, te.x1, te.b2);
-          tc.merge(tf.b1, tf.x1, tf.b2);
+#pragma unroll 2
           for (; r + WT < re; r += 2 * WT) {
             int d = r0 - r;
             if (d < 0) d += D;
