@@ -43,6 +43,8 @@ struct SrvRequest {
   std::string error;
   double t_submit = 0, t_admit = 0, t_done = 0;  // ms since the server started
   size_t bytes = 0;
+  int grid_ctas = 0;  // > 0: decoded on a grid of this many CTAs (chosen at admission for latency)
+  int sms = 0;        // SMs the request is counted as holding while it runs
   // in flight
   tv_model m = nullptr;
   cudaStream_t st = nullptr;
@@ -75,15 +77,35 @@ double now_ms(std::chrono::steady_clock::time_point t0) {
 
 // Smallest grid (head + workers) whose workers hold the window in shared
 // memory, times `spread` for speed; 0 if none.
-int grid_ctas_for(tv_model_s* m, int smem_optin, double spread) {
+int grid_ctas_nd(int N, int D, int sm_count, int smem_optin, double spread) {
   std::vector<int> first, count, base;
   std::vector<long long> wr;
   tv::GridParams P;
-  for (int G = 2; G <= m->sm_count; ++G) {
-    if (plan_grid(m, G, smem_optin, false, P, wr, first, count, base) && !P.w_global)
-      return std::min(m->sm_count, std::max(G, (int)std::ceil(G * spread)));
+  for (int G = 2; G <= sm_count; ++G) {
+    if (plan_grid_nd(N, D, G, smem_optin, false, P, wr, first, count, base) && !P.w_global)
+      return std::min(sm_count, std::max(G, (int)std::ceil(G * spread)));
   }
   return 0;
+}
+
+int grid_ctas_for(tv_model_s* m, int smem_optin, double spread) {
+  return grid_ctas_nd(m->N, m->D, m->sm_count, smem_optin, spread);
+}
+
+// Latency mode: while the device has SMs to spare and nothing else waits, a
+// long request is decoded on a grid of about 600 window cells per worker
+// (measured on GB300: at N=50, D=100 a step takes 13.2 us on one CTA, 2.8 us
+// on 16 CTAs; at N=50, D=1000, 2.8 us on the 24 CTAs its window needs and
+// 1.4 us on 96), at least the smallest grid that holds its window, at most
+// 96 CTAs.  This spends more SM time per request than the one-CTA kernel or
+// the smallest grid, so it is only taken below the load threshold; under load
+// the throughput-first choice stands.
+constexpr double kLatencyMinCells = 2e8;  // T*N*D below this finishes in tens of ms anyway
+int latency_grid_ctas(int N, int D, int sm_count, int smem_optin) {
+  const int g_min = grid_ctas_nd(N, D, sm_count, smem_optin, 1.0);
+  if (g_min <= 0) return 0;
+  const long long want = (long long)N * D / 600 + 2;
+  return (int)std::min<long long>(std::min(96, sm_count), std::max<long long>(g_min, want));
 }
 
 }  // namespace
@@ -105,7 +127,8 @@ struct tv_server_s {
   bool stop = false;
   bool hold = false;  // admission paused until the next completion
   uint64_t pool_keep_before = 0;  // the pool's retention setting before this server
-  int dev = 0, smem_optin = 0;
+  int dev = 0, smem_optin = 0, sm_count = 0;
+  int sms_busy = 0;  // SMs counted as held by the admitted requests
   std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
 
   // ---- scheduler thread ----
@@ -121,7 +144,10 @@ struct tv_server_s {
                              r->dur.data(), &r->m);
     if (rc == TV_OK) {
       const tv::CtaLayout L = tv::make_cta_layout(r->N, r->D);
-      if (L.bytes + 64 > (size_t)smem_optin) {
+      if (r->grid_ctas > 0) {
+        r->m->path_pref = TV_PATH_GRID;  // latency mode (admission chose the grid)
+        r->m->grid_ctas = r->grid_ctas;
+      } else if (L.bytes + 64 > (size_t)smem_optin) {
         const int G = grid_ctas_for(r->m, smem_optin, 1.5);
         r->m->path_pref = TV_PATH_GRID;
         r->m->grid_ctas = G;  // 0 (none fits shared memory): the whole GPU with the window in L2
@@ -214,9 +240,20 @@ struct tv_server_s {
         while (!hold && !pending.empty() && !free_slots.empty()) {
           SrvRequest* r = pending.front();
           const bool big = tv::make_cta_layout(r->N, r->D).bytes + 64 > (size_t)smem_optin;
-          const size_t need = request_bytes(*r, big, 16);
+          // latency mode when this request is the only one waiting and the
+          // SMs it would take are free (three quarters of the device at most)
+          int gl = 0;
+          if (pending.size() == 1 && (double)r->T * r->N * r->D >= kLatencyMinCells) {
+            gl = latency_grid_ctas(r->N, r->D, sm_count, smem_optin);
+            if (gl > 0 && sms_busy + gl > (3 * sm_count) / 4) gl = 0;
+          }
+          const int g_def = big ? std::max(1, grid_ctas_nd(r->N, r->D, sm_count, smem_optin, 1.5)) : 1;
+          const size_t need = request_bytes(*r, big || gl > 0, gl > 0 ? gl : (big ? g_def : 16));
           if (in_use + need > budget && !(running.empty() && to_start.empty())) break;
           pending.pop_front();
+          r->grid_ctas = gl;
+          r->sms = gl > 0 ? gl : g_def;
+          sms_busy += r->sms;
           const int slot = free_slots.back();
           free_slots.pop_back();
           r->st = streams[slot];
@@ -245,6 +282,8 @@ struct tv_server_s {
           r->status = TV_OK;
           r->error.clear();
           in_use -= r->bytes;
+          sms_busy -= r->sms;
+          r->sms = 0;
           for (size_t s2 = 0; s2 < streams.size(); ++s2)
             if (streams[s2] == r->st) free_slots.push_back((int)s2);
           r->st = nullptr;
@@ -254,6 +293,8 @@ struct tv_server_s {
           for (size_t q2 = to_start.size(); q2-- > q + 1;) {
             SrvRequest* o = to_start[q2];
             in_use -= o->bytes;
+            sms_busy -= o->sms;
+            o->sms = 0;
             for (size_t s2 = 0; s2 < streams.size(); ++s2)
               if (streams[s2] == o->st) free_slots.push_back((int)s2);
             o->st = nullptr;
@@ -288,6 +329,7 @@ struct tv_server_s {
         r->t_done = now_ms(t0);
         std::lock_guard<std::mutex> lk(mu);
         in_use -= r->bytes;
+        sms_busy -= r->sms;
         for (size_t s = 0; s < streams.size(); ++s)
           if (streams[s] == r->st) free_slots.push_back((int)s);
         r->st = nullptr;
@@ -319,6 +361,7 @@ tv_server tv_server_create(int64_t budget_bytes, int max_inflight) {
   tv_server_s* s = new tv_server_s();
   cudaGetDevice(&s->dev);
   cudaDeviceGetAttribute(&s->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->dev);
+  cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->dev);
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
   s->budget = budget_bytes > 0 ? (size_t)budget_bytes : (size_t)(0.8 * (double)free_b);

@@ -169,3 +169,29 @@ def test_models_return_all_device_memory(tvlib):
     free1, _ = torch.cuda.mem_get_info()
     # each churn allocates well over 100 MB (window-sum table, back-pointers)
     assert free0 - free1 < 32 << 20, (free0, free1)
+
+
+def test_server_latency_mode_for_a_long_request_alone(tvlib):
+    """A long request (T*N*D >= 2e8) that arrives alone at an idle server is
+    decoded on a grid of several CTAs instead of one CTA: the same result as
+    the decode alone and the oracle, in a fraction of the one-CTA time
+    (measured on GB300 at N=50, D=100: 13.2 us per step on one CTA, about
+    3.5 us on the 10 CTAs chosen)."""
+    import time
+    import tensor_viterbi.synthetic as syn
+    p = syn.discrete_problem(50, 100, 40000, 32, 5.0, 50.0, seed=17)
+    with tvlib.Model(*p.model_args()) as m:
+        m.set_path("cta")
+        m.decode(p.obs_seq)
+        t0 = time.perf_counter()
+        path_a, ll_a = m.decode(p.obs_seq, return_loglik=True)
+        cta_ms = 1e3 * (time.perf_counter() - t0)
+    with tvlib.Server() as srv:
+        srv.wait(srv.submit(*p.args()))  # warm-up of the grid kernel
+        path_s, ll_s, lat, queue = srv.wait(srv.submit(*p.args()))
+    np.testing.assert_array_equal(path_s, path_a)
+    assert ll_s == ll_a
+    ref = orc.decode(*p.args(), variant="omp")
+    np.testing.assert_array_equal(path_s, ref["path"])
+    assert ll_s == ref["loglik"]
+    assert lat - queue < 0.6 * cta_ms, (lat - queue, cta_ms)
