@@ -184,10 +184,11 @@ def prefix_for(w, cells_cap, longest):
 
 
 # CPU-baseline sample: the T-prefix 2D + 20000 (long enough for the window to
-# be fully rolled for 20000 steps), capped at ~1.1e10 window cells (about 30 s
-# of the host's cores); the reference arm's per-step sample is ~2e9 cells.
+# be fully rolled for 20000 steps), capped at ~1.1e10 window cells (about a
+# minute of a 16-core host); the reference arm's per-step sample is ~1.2e9
+# window cells (about 7 s), so that 25 of them take about three minutes.
 CPU_BASELINE_CELLS = 1.1e10
-REFERENCE_STEP_CELLS = 2.0e9
+REFERENCE_STEP_CELLS = 1.2e9
 # Parity check of the timed workload: the IEEE oracle on the T-prefix 2D + 2000.
 PARITY_CELLS = 6.0e9
 
