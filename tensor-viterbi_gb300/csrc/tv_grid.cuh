@@ -40,7 +40,7 @@
 namespace tv {
 
 constexpr int GRID_THREADS = 640;    // largest block (96 registers a thread)
-constexpr int WORKER_THREADS = 512;     // a worker CTA's scan threads: 16 warps (window in shared memory)
+constexpr int WORKER_THREADS = 256;     // a worker CTA's scan threads: 8 warps (window in shared memory)
 constexpr int WORKER_THREADS_GW = 512;  // 16 warps when the window is in global memory (more loads in flight)
 constexpr int WORKER_SERVICE = 64;      // + a certify warp and an intake warp; the rest of the CTA exits
 constexpr int GRID_L = 8;            // head candidates d < L (a power of two)
