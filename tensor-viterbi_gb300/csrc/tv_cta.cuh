@@ -125,6 +125,9 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
   double* tail = (double*)(base + L.o_tail);
   __shared__ int s_seq;
   __shared__ int s_bad;
+  // fraction bits f of the fixed point (scale = 2^f)
+  const int qf = (int)((__double_as_longlong(m.scale) >> 52) & 0x7ff) - 1023;
+  constexpr long long RESCORED = 1LL << 62;  // flag of a parked winner re-scored in phase 2
 
   // Model tables shared by every sequence of the batch.
   for (size_t k = threadIdx.x; k < (size_t)N * D; k += NTHREADS) qd[k] = m.qdurT[k];
@@ -233,44 +236,60 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
         tb.warp_reduce();
         __syncwarp();
 
+        // The certified argmax (d1, i1) is parked in dq[j] (dq is not read
+        // again before phase 3 overwrites it); an ambiguous state is re-scored
+        // exactly here by its warp and parked with its exact value in tail[j].
         const int d1 = tb.x1;
         int r1 = r0 - d1;
         if (r1 < 0) r1 += D;
         const unsigned short it = itil[(size_t)j * D + r1];
         const bool amb = (it & 0x8000) || ((tb.b1 - tb.b2) <= m.margin);
-        double vbest;
-        int bd, bi;
         if (!amb) {
-          const int i1 = it & 0x7fff;
-          const long long s1 = t - 1 - d1;
-          const double e = acc[(size_t)j * D + r1];
-          const double dp = dstar[(size_t)(s1 % (D + 1)) * N + i1];
-          vbest = (e + dp) + (m.trans[(size_t)j * N + i1] + m.durT[(size_t)j * D + d1]);
-          bd = d1;
-          bi = i1;
+          if (lane == 0) dq[j] = (long long)pack_psi(d1, it & 0x7fff);
         } else {
           const ExactBest eb = rescore_state(m, j, t, tau, r0, tb.b1 - m.margin, qd, ctil, acc, dstar, lane);
-          vbest = eb.value();
-          bd = eb.d;
-          bi = eb.i;
-        }
-        if (lane == 0) {
-          double* slot = dstar + (size_t)(t % (D + 1)) * N + j;
-          // For t < D the induction result replaces the initialisation value
-          // only when strictly larger (src/hsmm.cu:353-358).
-          double fin;
-          uint32_t w;
-          if (t >= D || vbest > *slot) {
-            fin = vbest;
-            w = pack_psi(bd, bi);
-          } else {
-            fin = *slot;
-            w = pack_psi((int)t, 0);
+          if (lane == 0) {
+            tail[j] = eb.value();
+            dq[j] = (long long)pack_psi(eb.d, eb.i) | RESCORED;
           }
-          *slot = fin;
-          dq[j] = quantize(fin, m.scale);
-          psi[(size_t)t * N + j] = w;
         }
+      }
+      __syncthreads();
+
+      // Phase 3: one lane per state, the exact score of each certified winner
+      // (src/hsmm.cu:341-346), the replacement rule for t < D (:353-358), the
+      // new delta row and back-pointers.  One lane per state keeps the FP64
+      // work of a step in few warp instructions (GB300 charges a warp-wide
+      // FP64 instruction the same pipe time however few lanes are active).
+      for (int j = threadIdx.x; j < N; j += NTHREADS) {
+        const long long w = dq[j];
+        const int bd = (int)((w >> 16) & 0xffff), bi = (int)(w & 0xffff);
+        double vbest;
+        if (w & RESCORED) {
+          vbest = tail[j];
+        } else {
+          int r1 = r0 - bd;
+          if (r1 < 0) r1 += D;
+          const long long s1 = t - 1 - bd;
+          const double e = acc[(size_t)j * D + r1];
+          const double dp = dstar[(size_t)(s1 % (D + 1)) * N + bi];
+          vbest = (e + dp) + (m.trans[(size_t)j * N + bi] + m.durT[(size_t)j * D + bd]);
+        }
+        double* slot = dstar + (size_t)(t % (D + 1)) * N + j;
+        // For t < D the induction result replaces the initialisation value
+        // only when strictly larger (src/hsmm.cu:353-358).
+        double fin;
+        uint32_t pw;
+        if (t >= D || vbest > *slot) {
+          fin = vbest;
+          pw = pack_psi(bd, bi);
+        } else {
+          fin = *slot;
+          pw = pack_psi((int)t, 0);
+        }
+        *slot = fin;
+        dq[j] = fixed_from_double(fin, qf);
+        psi[(size_t)t * N + j] = pw;
       }
       __syncthreads();
     }
