@@ -128,6 +128,8 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
   // fraction bits f of the fixed point (scale = 2^f)
   const int qf = (int)((__double_as_longlong(m.scale) >> 52) & 0x7ff) - 1023;
   constexpr long long RESCORED = 1LL << 62;  // flag of a parked winner re-scored in phase 2
+  int G = 1;  // lanes per state in the transition matvec
+  while (G < 32 && G * 4 < N) G <<= 1;
 
   // Model tables shared by every sequence of the batch.
   for (size_t k = threadIdx.x; k < (size_t)N * D; k += NTHREADS) qd[k] = m.qdurT[k];
@@ -197,12 +199,22 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
 
       // Phase 1: max-plus transition matvec for the newest predecessor slot
       // s = t-1, and the emission prefix P(t) = P(t-1) + qem[obs[t]].
-      for (int j = warp; j < N; j += NWARPS) {
+      // A group of G lanes per state (about four predecessors a lane, G a
+      // power of two up to a warp), so a small N takes few warps and few
+      // shuffle rounds.
+      for (int j0 = warp * (32 / G); j0 < N; j0 += NWARPS * (32 / G)) {
+        const int j = j0 + lane / G, u = lane % G;
         Top2 tb;
         tb.init();
-        for (int i = lane; i < N; i += 32) tb.push(qtr[(size_t)j * N + i] + dq[i], i);
-        tb.warp_reduce();
-        if (lane == 0) {
+        if (j < N)
+          for (int i = u; i < N; i += G) tb.push(qtr[(size_t)j * N + i] + dq[i], i);
+        for (int o = G >> 1; o > 0; o >>= 1) {
+          const long long ob1 = __shfl_xor_sync(0xffffffffu, tb.b1, o);
+          const long long ob2 = __shfl_xor_sync(0xffffffffu, tb.b2, o);
+          const int ox1 = __shfl_xor_sync(0xffffffffu, tb.x1, o);
+          tb.merge(ob1, ox1, ob2);
+        }
+        if (u == 0 && j < N) {
           ctil[(size_t)j * D + r0] = tb.b1 - ptil[j];
           const bool amb = (tb.b1 - tb.b2) <= m.margin;
           itil[(size_t)j * D + r0] = (unsigned short)(tb.x1 | (amb ? 0x8000 : 0));
