@@ -178,23 +178,9 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
     }
     __syncthreads();
 
-    // Per-step inputs loaded one step ahead when every thread serves one
-    // state in phase 1 and every warp one state in phase 2 (small N): the
-    // observation, the fixed-point emission of the phase-1 state and the
-    // exact emission of the phase-2 state.
-    const bool pf1 = N <= NWARPS * (32 / G);
-    const bool pf2 = N <= NWARPS;
-    const int j1 = warp * (32 / G) + lane / G;
-    int ot_cur = T > 1 ? obs[1] : 0;
-    long long qe_cur = 0;
-    double em_cur = 0.0;
-    if (pf1 && lane % G == 0 && j1 < N) qe_cur = m.qem[(size_t)ot_cur * N + j1];
-    if (pf2 && warp < N) em_cur = m.em[(size_t)ot_cur * N + warp];
-
     for (long long t = 1; t < T; ++t) {
       const int tau = (int)(t < D ? t : D);
-      const int ot = ot_cur;
-      const int ot_next = t + 1 < T ? obs[t + 1] : 0;  // used after phase 2
+      const int ot = obs[t];
       const int r0 = (int)((t - 1) % D);  // ring slot of s = t-1 (d = 0)
 
       // Phase 0 (t <= D): the reference rebuilds the window sums newest-first,
@@ -232,7 +218,7 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
           ctil[(size_t)j * D + r0] = tb.b1 - ptil[j];
           const bool amb = (tb.b1 - tb.b2) <= m.margin;
           itil[(size_t)j * D + r0] = (unsigned short)(tb.x1 | (amb ? 0x8000 : 0));
-          ptil[j] += pf1 ? qe_cur : m.qem[(size_t)ot * N + j];
+          ptil[j] += m.qem[(size_t)ot * N + j];
         }
       }
       __syncthreads();
@@ -241,7 +227,7 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
       // em_t with E_t[0] = 0 + em_t, src/hsmm.cu:298-310), the fixed-point
       // scan over d and the certified exact winner.
       for (int j = warp; j < N; j += NWARPS) {
-        const double emj = pf2 ? em_cur : m.em[(size_t)ot * N + j];
+        const double emj = m.em[(size_t)ot * N + j];
         Top2 tb;
         tb.init();
         if (t > D) {
@@ -280,12 +266,6 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
           }
         }
       }
-      // next step's inputs, in flight during phase 3
-      if (t + 1 < T) {
-        if (pf1 && lane % G == 0 && j1 < N) qe_cur = m.qem[(size_t)ot_next * N + j1];
-        if (pf2 && warp < N) em_cur = m.em[(size_t)ot_next * N + warp];
-      }
-      ot_cur = ot_next;
       __syncthreads();
 
       // Phase 3: one lane per state, the exact score of each certified winner
@@ -305,7 +285,7 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
           const long long s1 = t - 1 - bd;
           const double e = acc[(size_t)j * D + r1];
           const double dp = dstar[(size_t)(s1 % (D + 1)) * N + bi];
-          vbest = (e + dp) + (__ldg(m.trans + (size_t)j * N + bi) + __ldg(m.durT + (size_t)j * D + bd));
+          vbest = (e + dp) + (m.trans[(size_t)j * N + bi] + m.durT[(size_t)j * D + bd]);
         }
         double* slot = dstar + (size_t)(t % (D + 1)) * N + j;
         // For t < D the induction result replaces the initialisation value
