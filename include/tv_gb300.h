@@ -38,7 +38,9 @@ enum tv_status {
     TV_ECUDA = -7,      /* CUDA runtime error (see tv_last_error) */
     TV_EINTERNAL = -8,  /* device-side consistency check failed */
     TV_ENODEV = -9,     /* no CUDA device */
-    TV_ETIMEOUT = -10   /* a bounded device-side wait gave up (no progress) */
+    TV_ETIMEOUT = -10,  /* a bounded device-side wait gave up (no progress) */
+    TV_ENONPOS = -11    /* forward-backward: a normaliser or forward variable
+                           not positive (hsmmlearn's err = 1) */
 };
 
 /* Message for the last non-OK status returned on this thread. */
@@ -197,6 +199,25 @@ double tv_model_kernel_ms(tv_model m);
 int tv_decode_device_static(tv_model m, const int32_t* obs_dev, int64_t T,
                             int32_t* path_dev, double* loglik_dev, int* status_dev,
                             void* stream);
+
+/* ---- HSMM training: the forward-backward E step ----
+ *
+ * tv_fb replaces hsmmlearn's FBImpl (hsmmlearn/hsmmlearn/_hsmm/src/FBImpl.cpp)
+ * as called through its wrapper _fb_impl (hsmmlearn/hsmmlearn/base.pyx:50-)
+ * by HSMMModel.fit (hsmmlearn/hsmmlearn/hsmm.py:181-305) once per EM
+ * iteration.  Same arguments and layouts, host buffers, synchronous:
+ *   censoring  0 none, 1 right censoring (fit's default); 2 (left and right)
+ *              is not supported and returns TV_EINVAL
+ *   d (J, M)   duration pmf rows, entry u-1 = P(duration u)
+ *   p (J, J)   transition matrix [from][to]; pi (J); pdf (J, tau) likelihoods
+ *   outputs    F, L, G, L1, Norm (J, tau), N (tau), eta (J, M); G[:, 0] and
+ *              L1[:, tau-1] are not written (left as passed in)
+ * Returns TV_OK, or TV_ENONPOS where the reference reports err = 1.  Values
+ * agree with the reference to rounding (some products and sums associate
+ * differently), not bit for bit. */
+int tv_fb(int censoring, int64_t tau, int J, int M, const double* d, const double* p, const double* pi,
+          const double* pdf, double* F, double* L, double* G, double* L1, double* N, double* Norm,
+          double* eta);
 
 /* ---- Gaussian emissions (no reference counterpart: the reference takes a
  * discrete emission table only; a per-timestep table with obs = 0..T-1 is

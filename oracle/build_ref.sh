@@ -4,7 +4,7 @@
 # from the read-only reference checkout into oracle/_ref/.  Nothing is copied
 # into this repository: the sources are compiled where they lie.
 #
-# Three builds are produced:
+# Four builds are produced:
 #   oracle/_ref/shipped/_native*.so  the reference's own CPU flags
 #                                    (CMakeLists.txt:131-136: -O3 -march=native
 #                                    -mtune=native -ffast-math, OpenMP)
@@ -21,6 +21,8 @@
 #                                    under oracle/ref_cuda.c, a host driver
 #                                    written here that restates the reference's
 #                                    launch sequence (src/hsmm.cu:604-791).
+#   oracle/_ref/hsmmlearn/base*.so   hsmmlearn's compiled core (forward-backward
+#                                    of the EM fit), see build_hsmmlearn below
 #
 # Usage: oracle/build_ref.sh [REFERENCE_ROOT]
 # The reference checkout is the argument, else $TV_REFERENCE_ROOT, else the
@@ -86,7 +88,35 @@ build_cuda() {
     echo "build_ref: built $out/kernels_sm103a.cubin"
 }
 
+# The reference's training step: hsmmlearn's compiled core (its Cython
+# wrapper base.pyx over _hsmm/src/*.cpp, the forward-backward of
+# FBImpl.cpp), built as the Python extension oracle/_ref/hsmmlearn/base*.so
+# with the package's own flags (setup.py: -fopenmp), so that its Python
+# package under the checkout (hsmm.py's fit) can run against it.
+build_hsmmlearn() {
+    local out="$OUT/hsmmlearn"
+    local src="$REF/hsmmlearn/hsmmlearn"
+    if [[ ! -f "$src/base.pyx" ]]; then
+        echo "build_ref: hsmmlearn sources not found; skipping" >&2
+        return 0
+    fi
+    if ! "$PY" -c 'import Cython' 2>/dev/null; then
+        echo "build_ref: Cython not importable; hsmmlearn not built" >&2
+        return 0
+    fi
+    mkdir -p "$out"
+    local so="$out/base$SUFFIX"
+    if [[ -f "$so" && "$so" -nt "$src/base.pyx" && "$so" -nt "$src/_hsmm/src/FBImpl.cpp" ]]; then
+        return 0
+    fi
+    "$PY" -m cython --cplus -3 -o "$out/base.cpp" "$src/base.pyx"
+    g++ -O2 -fPIC -shared -fopenmp -isystem "$PY_INC" -I"$src" "$out/base.cpp" "$src"/_hsmm/src/*.cpp -o "$so.tmp"
+    mv "$so.tmp" "$so"
+    echo "build_ref: built $so"
+}
+
 build shipped -O3 -march=native -mtune=native -ffast-math &
 build ieee -O2 &
 build_cuda &
+build_hsmmlearn &
 wait

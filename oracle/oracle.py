@@ -51,6 +51,9 @@ def _load(name: str) -> C.CDLL:
         h.tvo_score_segments.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _ip, _ip, _bp]
         h.tvo_survival.restype = None
         h.tvo_survival.argtypes = [C.c_int, C.c_int, _dp, _dp]
+        if hasattr(h, "tvo_fb"):
+            h.tvo_fb.restype = C.c_int
+            h.tvo_fb.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int] + [_dp] * 11
         if hasattr(h, "tvo_decode_cuda"):
             h.tvo_decode_cuda.restype = C.c_int
             h.tvo_decode_cuda.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _ip, C.c_int,
@@ -237,6 +240,51 @@ def ref_cuda_decode(n_states, trans_mat, emission_probs, duration_probs_linear, 
     if rc != 0:
         raise RuntimeError(f"reference CUDA decode failed ({rc}): {h.tvr_last_error().decode()}")
     return dict(path=path, loglik=float(ll[0]), final=final, ms_call=float(ms[0]), ms_kernels=float(ms[1]))
+
+
+FB_KEYS = ("F", "L", "G", "L1", "N", "Norm", "eta")
+
+
+def forward_backward(censoring, d, p, pi, pdf):
+    """hsmmlearn's forward-backward (FBImpl.cpp) restated in C: d (J, M)
+    duration pmf, p (J, J) [from][to], pi (J), pdf (J, tau) likelihoods.
+    Returns dict(err, F, L, G, L1, N, Norm, eta) with hsmmlearn's layouts."""
+    h = _load("liboracle.so")
+    d, p, pi, pdf = _f64(d), _f64(p), _f64(pi).reshape(-1), _f64(pdf)
+    J, M = d.shape
+    tau = pdf.shape[1]
+    out = {k: np.zeros((J, tau)) for k in ("F", "L", "G", "L1", "Norm")}
+    out["N"] = np.zeros(tau)
+    out["eta"] = np.zeros((J, M))
+    rc = h.tvo_fb(int(censoring), tau, J, M, d.ctypes.data_as(_dp), p.ctypes.data_as(_dp), pi.ctypes.data_as(_dp),
+                  pdf.ctypes.data_as(_dp), *(out[k].ctypes.data_as(_dp) for k in FB_KEYS))
+    if rc < 0:
+        raise ValueError(f"oracle forward-backward: bad argument ({rc})")
+    out["err"] = int(rc)
+    return out
+
+
+def reference_hsmmlearn():
+    """The reference's hsmmlearn package (its Python modules from the
+    checkout, its compiled core from oracle/build_ref.sh), or None where
+    either is absent (the GPU host has no checkout)."""
+    root = reference_root()
+    d = HERE / "_ref" / "hsmmlearn"
+    so = sorted(d.glob("base*.so")) if d.exists() else []
+    if root is None or not so:
+        return None
+    if "hsmmlearn.hsmm" in sys.modules:
+        return sys.modules["hsmmlearn.hsmm"]
+    pkg_dir = root / "hsmmlearn"
+    if str(pkg_dir) not in sys.path:
+        sys.path.insert(0, str(pkg_dir))
+    spec = importlib.util.spec_from_file_location("hsmmlearn.base", str(so[0]))
+    base = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(base)
+    import hsmmlearn  # noqa: F401  (the package, from the checkout)
+    sys.modules["hsmmlearn.base"] = base
+    import hsmmlearn.hsmm as hh
+    return hh
 
 
 def reference_root() -> pathlib.Path | None:

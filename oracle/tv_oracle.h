@@ -44,6 +44,11 @@ int tvo_decode_cuda(int N, int O, int D, int T, const double* trans, const doubl
                     const int32_t* obs, int flags, const double* log_suffix, int nthreads,
                     int32_t* path, double* loglik, double* final);
 
+/* tv_fb_oracle.c: hsmmlearn's forward-backward (FBImpl.cpp), censoring 0/1. */
+int tvo_fb(int censoring, int tau, int J, int M, const double* d, const double* p, const double* pi,
+           const double* pdf, double* F, double* L, double* G, double* L1, double* Nn, double* Norm,
+           double* eta);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,196 @@
+// tv_fb.cuh -- the forward-backward E step of HSMM training on the GPU.
+//
+// The reference's training step is hsmmlearn's EM fit
+// (hsmmlearn/hsmmlearn/hsmm.py:181-305), whose E step is FBImpl
+// (hsmmlearn/hsmmlearn/_hsmm/src/FBImpl.cpp): Guedon's scaled forward and
+// backward recursions for an explicit-duration HSMM, then the expected
+// duration counts eta.  This kernel computes the same arrays with the same
+// formulas; one CTA runs one sequence, a warp per state (lanes over the
+// durations u) for the O(J*M) sums of a step, a thread per state for the
+// O(J) normalisation and transition sums, which keep the reference's
+// sequential order (j, i or k ascending).
+//
+// The products of likelihood ratios r_s = pdf[j][s] / N[s] over a segment
+// are kept in a ring per state, indexed by the segment's first (forward) or
+// last (backward) step, and multiplied by the new ratio every step (one
+// multiply per cell, like the decoder's window folds), instead of being
+// rebuilt for every u as the reference does; and the sums over u are lane
+// partials reduced by shuffles.  Both change the association of some
+// products and sums, so results agree with the reference to rounding
+// (relative differences of order 1e-14 on the tests' sequences), not bit for
+// bit.  The eta sums keep the reference's order over t, and the backward
+// right-censoring product s is formed in the reference's order.
+//
+// Censoring 0 (none) and 1 (right censoring, the fit's default) are
+// supported; the reference's left-censoring variant (2) is not.
+//
+// This file is included by tv_host.cu.
+#pragma once
+
+namespace tv {
+
+struct FbArgs {
+  int censoring, tau, J, M;
+  const double* d;    // (J, M) duration pmf, entry u-1 = P(duration u)
+  const double* p;    // (J, J) [from][to]
+  const double* pi;   // (J)
+  const double* pdf;  // (J, tau)
+  double *F, *L, *G, *L1, *N, *Norm, *eta;  // outputs, hsmmlearn's layouts
+  double* S;          // (J, tau) scratch: StateIn
+  double* D;          // (J, M+1) scratch: survival D[j][u] = sum_{v >= u} d[j][v]
+  double* ring;       // (2, J, M) scratch when the rings do not fit shared memory
+  int rings_in_smem;
+  int* status;        // 0, or 1 where the reference throws var_nonpositive_exception
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__global__ void __launch_bounds__(1024) fb_kernel(FbArgs a) {
+  extern __shared__ __align__(16) unsigned char fsm[];
+  const int J = a.J, M = a.M, tau = a.tau;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const bool right = a.censoring == 1;
+  double* Pf = a.rings_in_smem ? (double*)fsm : a.ring;  // [J][M] forward ring, by segment start s % M
+  double* Pb = Pf + (size_t)J * M;                         // [J][M] backward ring, by segment end e % M
+  __shared__ int s_bad;
+  __shared__ double s_N;
+  auto at = [&](double* x, int j, long long t) -> double& { return x[(size_t)j * tau + t]; };
+  auto atc = [&](const double* x, int j, long long t) -> double { return x[(size_t)j * tau + t]; };
+  auto dd = [&](int j, int u) -> double { return a.d[(size_t)j * M + (u - 1)]; };       // d[j][u], u = 1..M
+  auto DD = [&](int j, int u) -> double { return u <= M ? a.D[(size_t)j * (M + 1) + u] : 0.0; };
+  auto pp = [&](int i, int j) -> double { return a.p[(size_t)i * J + j]; };
+
+  if (tid == 0) s_bad = 0;
+  // CalcStoreD (dCalc.cpp:5-30): each sum from v = u upwards, as there
+  for (int j = warp; j < J; j += nw)
+    for (int u = lane + 1; u <= M; u += 32) {
+      double x = 0;
+      for (int v = u; v <= M; ++v) x += dd(j, v);
+      a.D[(size_t)j * (M + 1) + u] = x;
+    }
+  for (int j = warp; j < J; j += nw)
+    for (int u = lane + 1; u <= M; u += 32) a.eta[(size_t)j * M + (u - 1)] = 0.0;
+  __syncthreads();
+
+  // ---- forward recursion (FBImpl.cpp:62-140) ----
+  for (int t = 0; t < tau; ++t) {
+    for (int j = tid; j < J; j += blockDim.x)
+      at(a.Norm, j, t) = t == 0 ? atc(a.pdf, j, 0) * a.pi[j]
+                                : atc(a.pdf, j, t) * (at(a.S, j, t) - at(a.F, j, t - 1) + at(a.Norm, j, t - 1));
+    __syncthreads();
+    if (tid == 0) {
+      double n = 0;
+      for (int j = 0; j < J; ++j) n += at(a.Norm, j, t);
+      a.N[t] = n;
+      s_N = n;
+      if (!(n > 0)) s_bad = 1;
+    }
+    __syncthreads();
+    if (s_bad) break;
+    const double Nt = s_N;
+    for (int j = tid; j < J; j += blockDim.x) at(a.Norm, j, t) /= Nt;
+    // F[j][t] = sum_u P(t-u+1..t) * dur(u) * StateIn[j][t-u+1] (the segment
+    // that started at s = 0 takes pi instead); the last step takes the
+    // survival D instead of d
+    const bool last = t == tau - 1;
+    const int umax = min(t + 1, M);
+    for (int j = warp; j < J; j += nw) {
+      const double r = atc(a.pdf, j, t) / Nt;
+      double* P = Pf + (size_t)j * M;
+      double part = 0.0;
+      for (int u = lane + 1; u <= umax; u += 32) {
+        const int s = t - u + 1;
+        const int slot = s % M;
+        const double ob = (u == 1) ? r : P[slot] * r;
+        P[slot] = ob;
+        const double du = last ? DD(j, u) : dd(j, u);
+        part += (s > 0) ? ob * du * at(a.S, j, s) : ob * du * a.pi[j];
+      }
+      const double f = warp_sum(part);
+      if (lane == 0) {
+        at(a.F, j, t) = f;
+        if (!(f > 0)) s_bad = 1;
+      }
+    }
+    __syncthreads();
+    if (s_bad) break;
+    if (t < tau - 1)
+      for (int j = tid; j < J; j += blockDim.x) {
+        double x = 0;
+        for (int i = 0; i < J; ++i) x += pp(i, j) * at(a.F, i, t);
+        at(a.S, j, t + 1) = x;
+      }
+    __syncthreads();
+  }
+  if (s_bad) {
+    if (tid == 0) *a.status = 1;
+    return;
+  }
+
+  // ---- backward recursion (FBImpl.cpp:142-178) with eta (:231-270) ----
+  for (int j = tid; j < J; j += blockDim.x) at(a.L, j, tau - 1) = at(a.F, j, tau - 1);
+  __syncthreads();
+  for (int t = tau - 2; t >= 0; --t) {
+    const int span = tau - 1 - t;  // steps after t
+    const int umax = min(span, M);
+    for (int j = warp; j < J; j += nw) {
+      const double r = atc(a.pdf, j, t + 1) / a.N[t + 1];
+      double* Q = Pb + (size_t)j * M;
+      // A = sum_{i != j} p[i][j] F[i][t] (the eta weight of this step)
+      double A = 0;
+      for (int i = 0; i < J; ++i)
+        if (i != j) A += pp(i, j) * at(a.F, i, t);
+      double part = 0.0;
+      for (int u = lane + 1; u <= umax; u += 32) {
+        const int e = t + u;  // the segment t+1..e
+        const int slot = e % M;
+        const double ob = (u == 1) ? r : Q[slot] * r;
+        Q[slot] = ob;
+        const double h = (u < span) ? at(a.L1, j, e) * ob * dd(j, u) / at(a.F, j, e) : ob * DD(j, span);
+        part += h;
+        // eta: H term for u <= span - 1, right-censored term for u = span
+        if (u <= span - 1) a.eta[(size_t)j * M + (u - 1)] += A * h;
+      }
+      // right censoring: u >= span, the product over t+1..tau-1 (the
+      // reference's s, formed backwards: the ring entry of e = tau-1)
+      if (right && span <= M) {
+        __syncwarp();  // the lane that owns u = span wrote the entry
+        const double s_t = Q[(tau - 1) % M];
+        for (int u = lane + 1; u <= M; u += 32)
+          if (u >= span) a.eta[(size_t)j * M + (u - 1)] += A * (s_t * dd(j, u));
+      }
+      const double g = warp_sum(part);
+      if (lane == 0) at(a.G, j, t + 1) = g;
+    }
+    __syncthreads();
+    for (int j = tid; j < J; j += blockDim.x) {
+      double x = 0;
+      for (int k = 0; k < J; ++k) x += at(a.G, k, t + 1) * pp(j, k);
+      x *= at(a.F, j, t);
+      at(a.L1, j, t) = x;
+      at(a.L, j, t) = x + at(a.L, j, t + 1) - at(a.G, j, t + 1) * at(a.S, j, t + 1);
+    }
+    __syncthreads();
+  }
+
+  // eta: the segment that starts at t = 0 (FBImpl.cpp:252-266)
+  for (int j = warp; j < J; j += nw)
+    for (int u = lane + 1; u <= M; u += 32) {
+      if (!(right || u <= tau - 1)) continue;
+      double r = dd(j, u) * a.pi[j];
+      if (u <= tau - 1) {
+        for (int v = 1; v <= u; ++v) r *= atc(a.pdf, j, u - v) / a.N[u - v];
+        r *= at(a.L1, j, u - 1) / at(a.F, j, u - 1);
+      } else {
+        for (int v = 1; v <= tau; ++v) r *= atc(a.pdf, j, tau - v) / a.N[tau - v];
+      }
+      a.eta[(size_t)j * M + (u - 1)] += r;
+    }
+  if (tid == 0) *a.status = 0;
+}
+
+}  // namespace tv

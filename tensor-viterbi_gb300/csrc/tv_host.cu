@@ -28,6 +28,7 @@
 #include "tv_cta.cuh"
 #include "tv_grid.cuh"
 #include "tv_floor.cuh"
+#include "tv_fb.cuh"
 
 namespace {
 
@@ -881,6 +882,92 @@ int read_status(tv_model_s* m, int n_seq, cudaStream_t st) {
   return TV_OK;
 }
 
+// Device buffers freed together when the arena goes out of scope.
+struct DevArena {
+  std::vector<void*> p;
+  DevArena() = default;
+  DevArena(const DevArena&) = delete;
+  DevArena& operator=(const DevArena&) = delete;
+  ~DevArena() {
+    for (void* q : p) cudaFree(q);
+  }
+  template <class T>
+  int get(T** out, size_t n) {
+    void* q = nullptr;
+    if (cudaMalloc(&q, sizeof(T) * std::max<size_t>(n, 1)) != cudaSuccess) {
+      cudaGetLastError();
+      return TV_ENOMEM;
+    }
+    p.push_back(q);
+    *out = (T*)q;
+    return TV_OK;
+  }
+};
+
+// The forward-backward E step (tv_fb): device copies of the inputs and
+// outputs, one launch, copies back.
+int fb_run(int censoring, int64_t tau, int J, int M, const double* d, const double* p, const double* pi,
+           const double* pdf, double* F, double* L, double* G, double* L1, double* Nn, double* Norm,
+           double* eta) {
+  if (censoring != 0 && censoring != 1)
+    return fail(TV_EINVAL, "tv_fb: censoring must be 0 (none) or 1 (right); left censoring (2) is not supported");
+  if (tau < 1 || tau > 0x7fffffffLL || J < 1 || J > 1024 || M < 1)
+    return fail(TV_EINVAL, "tv_fb: need tau >= 1, 1 <= J <= 1024, M >= 1");
+  if (!d || !p || !pi || !pdf || !F || !L || !G || !L1 || !Nn || !Norm || !eta)
+    return fail(TV_EINVAL, "tv_fb: null argument");
+  int devs = 0;
+  if (cudaGetDeviceCount(&devs) != cudaSuccess || devs == 0) return fail(TV_ENODEV, "no CUDA device");
+  const size_t JT = (size_t)J * (size_t)tau, JM = (size_t)J * M;
+  DevArena b;
+  double *dd, *dp, *dpi, *dpdf, *dF, *dL, *dG, *dL1, *dN, *dNorm, *deta, *dS, *dD, *dring = nullptr;
+  int* dst;
+  if (b.get(&dd, JM) || b.get(&dp, (size_t)J * J) || b.get(&dpi, J) || b.get(&dpdf, JT) || b.get(&dF, JT) ||
+      b.get(&dL, JT) || b.get(&dG, JT) || b.get(&dL1, JT) || b.get(&dN, (size_t)tau) || b.get(&dNorm, JT) ||
+      b.get(&deta, JM) || b.get(&dS, JT) || b.get(&dD, (size_t)J * (M + 1)) || b.get(&dst, 1))
+    return fail(TV_ENOMEM, "tv_fb: device allocation failed");
+  int dev = 0, smem_optin = 0;
+  TV_CUDA(cudaGetDevice(&dev));
+  TV_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const size_t ring_bytes = 2 * JM * sizeof(double);
+  const bool in_smem = ring_bytes + 1024 <= (size_t)smem_optin;
+  if (!in_smem && b.get(&dring, 2 * JM)) return fail(TV_ENOMEM, "tv_fb: device allocation failed");
+  TV_CUDA(cudaMemcpy(dd, d, sizeof(double) * JM, cudaMemcpyHostToDevice));
+  TV_CUDA(cudaMemcpy(dp, p, sizeof(double) * J * J, cudaMemcpyHostToDevice));
+  TV_CUDA(cudaMemcpy(dpi, pi, sizeof(double) * J, cudaMemcpyHostToDevice));
+  TV_CUDA(cudaMemcpy(dpdf, pdf, sizeof(double) * JT, cudaMemcpyHostToDevice));
+  // the columns the recursions do not write stay as the caller passed them
+  // (hsmmlearn hands in zeroed arrays): G[:, 0], L1[:, tau-1]
+  TV_CUDA(cudaMemcpy(dG, G, sizeof(double) * JT, cudaMemcpyHostToDevice));
+  TV_CUDA(cudaMemcpy(dL1, L1, sizeof(double) * JT, cudaMemcpyHostToDevice));
+  TV_CUDA(cudaMemset(dS, 0, sizeof(double) * JT));
+  tv::FbArgs A{};
+  A.censoring = censoring; A.tau = (int)tau; A.J = J; A.M = M;
+  A.d = dd; A.p = dp; A.pi = dpi; A.pdf = dpdf;
+  A.F = dF; A.L = dL; A.G = dG; A.L1 = dL1; A.N = dN; A.Norm = dNorm; A.eta = deta;
+  A.S = dS; A.D = dD; A.ring = dring; A.rings_in_smem = in_smem ? 1 : 0; A.status = dst;
+  const int threads = 32 * std::min(32, J);
+  const size_t dyn = in_smem ? ring_bytes : 0;
+  if (dyn) {
+    int rc = raise_smem_limit((const void*)tv::fb_kernel);
+    if (rc != TV_OK) return rc;
+  }
+  tv::fb_kernel<<<1, threads, dyn>>>(A);
+  TV_CUDA(cudaGetLastError());
+  int st = 0;
+  TV_CUDA(cudaMemcpy(&st, dst, sizeof(int), cudaMemcpyDeviceToHost));
+  TV_CUDA(cudaMemcpy(F, dF, sizeof(double) * JT, cudaMemcpyDeviceToHost));
+  TV_CUDA(cudaMemcpy(L, dL, sizeof(double) * JT, cudaMemcpyDeviceToHost));
+  TV_CUDA(cudaMemcpy(G, dG, sizeof(double) * JT, cudaMemcpyDeviceToHost));
+  TV_CUDA(cudaMemcpy(L1, dL1, sizeof(double) * JT, cudaMemcpyDeviceToHost));
+  TV_CUDA(cudaMemcpy(Nn, dN, sizeof(double) * tau, cudaMemcpyDeviceToHost));
+  TV_CUDA(cudaMemcpy(Norm, dNorm, sizeof(double) * JT, cudaMemcpyDeviceToHost));
+  TV_CUDA(cudaMemcpy(eta, deta, sizeof(double) * JM, cudaMemcpyDeviceToHost));
+  if (st != 0)
+    return fail(TV_ENONPOS, "forward-backward: a normaliser or forward variable is not positive");
+  return TV_OK;
+}
+
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -1342,6 +1429,12 @@ int tv_decode_device_static(tv_model m, const int32_t* obs_dev, int64_t T, int32
   if (status_dev) static_status_kernel<<<1, 1, 0, st>>>(status, status_dev);
   TV_CUDA(cudaGetLastError());
   return TV_OK;
+}
+
+int tv_fb(int censoring, int64_t tau, int J, int M, const double* d, const double* p, const double* pi,
+          const double* pdf, double* F, double* L, double* G, double* L1, double* Nn, double* Norm,
+          double* eta) {
+  return fb_run(censoring, tau, J, M, d, p, pi, pdf, F, L, G, L1, Nn, Norm, eta);
 }
 
 int tv_step_floor(int n_states, int max_dur, int64_t steps, double* out) {

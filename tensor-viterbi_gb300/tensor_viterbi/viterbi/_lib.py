@@ -24,6 +24,7 @@ TV_ECUDA = -7
 TV_EINTERNAL = -8
 TV_ENODEV = -9
 TV_ETIMEOUT = -10
+TV_ENONPOS = -11
 
 # Argument errors surface as ValueError (the caller passed something the
 # decoder cannot accept); runtime failures as RuntimeError.
@@ -54,6 +55,7 @@ EXPORTS = {
     "tv_model_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "tv_model_kernel_ms": (C.c_double, [C.c_void_p]),
     "tv_step_floor": (C.c_int, [C.c_int, C.c_int, C.c_int64, _dp]),
+    "tv_fb": (C.c_int, [C.c_int, C.c_int64, C.c_int, C.c_int] + [_dp] * 11),
     "tv_decode_device_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p]),
     "tv_gaussian_loglik": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, _dp, _dp, C.c_void_p, C.c_void_p]),

@@ -380,3 +380,31 @@ def step_floor(n_states: int, max_dur: int, steps: int = 20000) -> dict:
     return {"chain_clocks_per_step": float(out[0]), "chain_us_per_step": float(out[1]),
             "roundtrip_clocks": float(out[2]), "roundtrip_us": float(out[3]), "matvec_split": bool(out[4]),
             "roundtrip_sms": [int(out[5]), int(out[6])]}
+
+
+def forward_backward(censoring, d, p, pi, pdf) -> dict:
+    """The forward-backward E step of HSMM training on the GPU (tv_fb), with
+    hsmmlearn's _fb_impl arguments and layouts (hsmmlearn/hsmmlearn/base.pyx):
+    censoring 0 or 1, d (J, M) duration pmf, p (J, J) [from][to], pi (J),
+    pdf (J, tau) likelihoods.  Returns dict(err, F, L, G, L1, N, Norm, eta):
+    err = 1 where the reference reports a non-positive normaliser or forward
+    variable, as its _fb_impl does; other failures raise."""
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    pi = np.ascontiguousarray(pi, dtype=np.float64).reshape(-1)
+    pdf = np.ascontiguousarray(pdf, dtype=np.float64)
+    J, M = d.shape
+    tau = pdf.shape[1]
+    if p.shape != (J, J) or pi.shape != (J,) or pdf.shape[0] != J:
+        raise ValueError("forward_backward: shapes must be d (J, M), p (J, J), pi (J), pdf (J, tau)")
+    out = {k: np.zeros((J, tau)) for k in ("F", "L", "G", "L1", "Norm")}
+    out["N"] = np.zeros(tau)
+    out["eta"] = np.zeros((J, M))
+    rc = _lib.lib().tv_fb(int(censoring), tau, J, M, _lib.dptr(d), _lib.dptr(p), _lib.dptr(pi), _lib.dptr(pdf),
+                          *(_lib.dptr(out[k]) for k in ("F", "L", "G", "L1", "N", "Norm", "eta")))
+    if rc == _lib.TV_ENONPOS:
+        out["err"] = 1
+        return out
+    _lib.check(rc)
+    out["err"] = 0
+    return out

@@ -1,0 +1,70 @@
+"""HSMM training step on the GPU: the forward-backward kernel (tv_fb) against
+the reference's own outputs (tests/golden/fb/) and the oracle, and the EM fit
+with the GPU E step against the reference's HSMMModel.fit.  Tolerance: the
+kernel associates some products and sums differently from the reference
+(rings of likelihood-ratio products, lane-parallel sums over durations), so
+arrays agree to a relative 1e-10 and the fitted parameters to 1e-8."""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle import oracle as orc
+from test_fb import FB, _model, check_fit, em_cases, fb_cases
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+
+
+def _close(got, want, name):
+    scale = np.maximum(np.abs(want), np.abs(want).max() * 1e-12 + 1e-300)
+    err = np.abs(got - want) / scale
+    assert err.max() <= RTOL, (name, float(err.max()))
+
+
+@pytest.mark.parametrize("name", fb_cases())
+def test_gpu_forward_backward_matches_the_reference(tvlib, name):
+    z = np.load(FB / f"{name}.npz")
+    r = tvlib.forward_backward(int(z["censoring"]), z["d"], z["p"], z["pi"], z["pdf"])
+    assert r["err"] == int(z["err"])
+    for k in orc.FB_KEYS:
+        _close(r[k], z[k], k)
+
+
+@pytest.mark.parametrize("J,M,tau,cens", [(20, 200, 3000, 1), (7, 333, 1200, 0), (40, 64, 2000, 1), (3, 5, 4000, 1)])
+def test_gpu_forward_backward_matches_the_oracle_on_random_models(tvlib, J, M, tau, cens):
+    rng = np.random.default_rng(J * 1000 + M)
+    p = rng.dirichlet(np.ones(J), size=J)
+    d = rng.dirichlet(np.ones(M) * 1.5, size=J)
+    pi = rng.dirichlet(np.ones(J))
+    pdf = rng.uniform(0.01, 1.0, size=(J, tau))
+    want = orc.forward_backward(cens, d, p, pi, pdf)
+    got = tvlib.forward_backward(cens, d, p, pi, pdf)
+    assert got["err"] == want["err"] == 0
+    for k in orc.FB_KEYS:
+        _close(got[k], want[k], k)
+
+
+def test_gpu_forward_backward_reports_a_zero_normaliser(tvlib):
+    z = np.load(FB / "fb_J3_M20_T300_c1.npz")
+    pdf = z["pdf"].copy()
+    pdf[:, 7] = 0.0
+    assert tvlib.forward_backward(1, z["d"], z["p"], z["pi"], pdf)["err"] == 1
+    # and the next call is unaffected
+    r = tvlib.forward_backward(1, z["d"], z["p"], z["pi"], z["pdf"])
+    assert r["err"] == 0
+    _close(r["N"], z["N"], "N")
+
+
+def test_gpu_forward_backward_refuses_left_censoring(tvlib):
+    z = np.load(FB / "fb_J3_M20_T300_c1.npz")
+    with pytest.raises(ValueError, match="censoring"):
+        tvlib.forward_backward(2, z["d"], z["p"], z["pi"], z["pdf"])
+
+
+@pytest.mark.parametrize("name", em_cases())
+def test_gpu_em_fit_matches_the_reference_fit(tvlib, name):
+    z = np.load(FB / f"{name}.npz")
+    model = _model(z)
+    conv, llh = model.fit(z["obs"], max_iter=int(z["max_iter"]), censoring=bool(z["censoring"]))
+    check_fit(model, z, conv, llh, rtol=1e-8)
