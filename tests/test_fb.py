@@ -43,14 +43,17 @@ def _model(z):
     return hsmm_em.GaussianHSMM(z["means"], z["scales"], z["durations0"], z["tmat0"], startprob=z["startprob0"])
 
 
-def check_fit(model, z, conv, llh, rtol):
+def check_fit(model, z, conv, llh, rtol, atol):
+    """Fitted parameters against the reference's: relative rtol, and atol for
+    the probabilities near zero (start and duration probabilities floored at
+    1e-14 or vanishing), whose relative error is large at any precision."""
     assert conv == bool(z["converged"])
     np.testing.assert_allclose(llh, float(z["llh"]), rtol=rtol)
-    np.testing.assert_allclose(model.tmat, z["fit_tmat"], rtol=rtol, atol=1e-300)
-    np.testing.assert_allclose(model.durations, z["fit_durations"], rtol=rtol, atol=1e-300)
-    np.testing.assert_allclose(model.startprob, z["fit_startprob"], rtol=rtol, atol=1e-300)
+    np.testing.assert_allclose(model.tmat, z["fit_tmat"], rtol=rtol, atol=atol)
+    np.testing.assert_allclose(model.durations, z["fit_durations"], rtol=rtol, atol=atol)
+    np.testing.assert_allclose(model.startprob, z["fit_startprob"], rtol=rtol, atol=atol)
     if str(z["kind"]) == "multinomial":
-        np.testing.assert_allclose(model.probabilities, z["fit_emissions"], rtol=rtol)
+        np.testing.assert_allclose(model.probabilities, z["fit_emissions"], rtol=rtol, atol=atol)
     else:
         np.testing.assert_allclose(model.means, z["fit_means"], rtol=rtol)
         np.testing.assert_allclose(model.scales, z["fit_scales"], rtol=rtol)
@@ -62,7 +65,9 @@ def test_em_with_the_oracle_e_step_equals_the_reference_fit(name):
     model = _model(z)
     conv, llh = model.fit(z["obs"], max_iter=int(z["max_iter"]), censoring=bool(z["censoring"]),
                           forward_backward=orc.forward_backward)
-    check_fit(model, z, conv, llh, rtol=1e-12)
+    # the fixtures were made on x86; scipy's densities and numpy's sums differ
+    # in the last bits on other hosts
+    check_fit(model, z, conv, llh, rtol=1e-10, atol=1e-14)
 
 
 def test_em_restores_the_parameters_when_the_e_step_fails():
