@@ -52,6 +52,9 @@ WORKLOADS = {
     "single_N100_D10000_T1e7": dict(N=100, D=10_000, T=10_000_000, M=64, lo=5.0, hi=50.0, seed=4),
     # 4096 sequences sharing one model, lengths log-uniform in [1e3, 1e5]
     "batch_4096_N10_D250": dict(kind="batch", n_seq=4096, N=10, D=250, M=16, lo=1e3, hi=1e5, seed=2),
+    # the training step: one forward-backward E step of hsmmlearn's EM fit
+    # (FBImpl.cpp) on one sequence, J states, M durations, T observations
+    "fb_J10_M100_T1e5": dict(kind="fb", J=10, M=100, T=100_000, K=16, seed=5),
     # served: Poisson arrivals of requests with their own models; N from
     # {10,15,25,50}, D from {100,250,500,1000}, T log-uniform in [1e3, 1e6],
     # half discrete (M = 32), half Gaussian; arrival rates at fractions of the
@@ -232,6 +235,76 @@ def run_reference(args, w, wname):
         "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def fb_problem(w):
+    """A seeded HSMM (Dirichlet transition, duration and emission rows, zero
+    self-transitions) and a sequence sampled from it; returns (d, p, pi, pdf)
+    in hsmmlearn's _fb_impl layouts, pdf the emission likelihoods."""
+    import numpy as np
+    import tensor_viterbi.synthetic as syn
+    rng = np.random.default_rng(w["seed"])
+    J, M, T, K = w["J"], w["M"], w["T"], w["K"]
+    lm = syn.random_model(rng, J, M, K, 5.0, M / 2.0)
+    states = syn.sample_states(rng, lm, T)
+    obs = syn.sample_discrete_obs(rng, lm.B, states)
+    pdf = np.ascontiguousarray(lm.B[:, obs])
+    pdf[pdf < 1e-12] = 1e-12
+    return np.ascontiguousarray(lm.P), np.ascontiguousarray(lm.A), lm.pi, pdf
+
+
+def run_fb(args, w, wname):
+    """The forward-backward E step (tv_fb) through its host-buffer call, as
+    hsmmlearn's fit makes it: inputs copied in, outputs copied out, both in
+    the timed region; cells = T*J*M per pass.  CPU baseline: the oracle's
+    restatement of FBImpl.cpp (serial, bit-exact to the reference's build)."""
+    import numpy as np
+    import torch
+    from tensor_viterbi.viterbi import native
+    ws, rank, _ = dist_env()
+    torch.cuda.set_device(0)
+    native.configure("gb300", "cuda")
+    d, p, pi, pdf = fb_problem(w)
+    J, M, T = w["J"], w["M"], w["T"]
+    cells = T * J * M
+    for _ in range(args.warmup):
+        native.forward_backward(1, d, p, pi, pdf)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    secs = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        r = native.forward_backward(1, d, p, pi, pdf)
+        secs.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+    value = cells * len(secs) / sum(secs)
+    cpu = parity = None
+    if not args.no_cpu_baseline or not args.no_parity:
+        from oracle import oracle as orc
+        t0 = time.perf_counter()
+        ref = orc.forward_backward(1, d, p, pi, pdf)
+        dt = time.perf_counter() - t0
+        cpu = {"value": cells / dt, "unit": "cells/s", "cores": 1, "kind": "port",
+               "sample": f"the whole workload ({dt:.1f} s): the serial C restatement of hsmmlearn's FBImpl.cpp, "
+                         f"bit-exact to the reference's own build"}
+        big = {k: float(np.abs(ref[k]).max()) for k in orc.FB_KEYS}
+        parity = {"err_equal": r["err"] == ref["err"],
+                  "max_err_over_max_entry": max(float(np.abs(r[k] - ref[k]).max()) / big[k] for k in orc.FB_KEYS),
+                  "oracle": "C restatement of hsmmlearn FBImpl.cpp"}
+    io = (J * M + J * J + J + J * T) * 8 + 2 * J * T * 8
+    line = {"metric": "T*J*M cells/s (HSMM forward-backward E step, FP64)", "value": value, "unit": "cells/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wname, "states": J, "durations": M, "T": T, "symbols": w["K"], "censoring": 1,
+                       "form": "one sequence, host buffers (hsmmlearn's _fb_impl call)",
+                       "l2": "inputs (J*T likelihoods) larger than L2 are re-copied every step"},
+            "cpu_baseline": cpu, "parity": parity,
+            "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": io,
+                    "d2h_bytes_per_step": (5 * J * T + T + J * M) * 8},
+            "gpu_launches": args.steps, "clocks": clk}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -807,6 +880,12 @@ def main():
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no served form; its arm is measured on the single-sequence workload"}))
             return 0
         return run_served(args, w, args.workload)
+    if w.get("kind") == "fb":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference arm is measured on the "
+                              "single-sequence decode workload"}))
+            return 0
+        return run_fb(args, w, args.workload)
     if w.get("kind") == "batch":
         if args.impl == "reference":
             return run_reference_batch(args, w, args.workload)
