@@ -39,7 +39,10 @@ struct FbArgs {
   double* S;          // (J, tau) scratch: StateIn
   double* D;          // (J, M+1) scratch: survival D[j][u] = sum_{v >= u} d[j][v]
   double* ring;       // (2, J, M) scratch when the rings do not fit shared memory
+                      // (fb_small_kernel: (4, J, M))
   int rings_in_smem;
+  double* R;          // (J, tau) scratch of fb_small_kernel: r = pdf / N
+  double* A;          // (J, tau) scratch of fb_small_kernel: sum_{i != j} p[i][j] F[i][t]
   int* status;        // 0, or 1 where the reference throws var_nonpositive_exception
 };
 
@@ -178,6 +181,180 @@ __global__ void __launch_bounds__(1024) fb_kernel(FbArgs a) {
   }
 
   // eta: the segment that starts at t = 0 (FBImpl.cpp:252-266)
+  for (int j = warp; j < J; j += nw)
+    for (int u = lane + 1; u <= M; u += 32) {
+      if (!(right || u <= tau - 1)) continue;
+      double r = dd(j, u) * a.pi[j];
+      if (u <= tau - 1) {
+        for (int v = 1; v <= u; ++v) r *= atc(a.pdf, j, u - v) / a.N[u - v];
+        r *= at(a.L1, j, u - 1) / at(a.F, j, u - 1);
+      } else {
+        for (int v = 1; v <= tau; ++v) r *= atc(a.pdf, j, tau - v) / a.N[tau - v];
+      }
+      a.eta[(size_t)j * M + (u - 1)] += r;
+    }
+  if (tid == 0) *a.status = 0;
+}
+
+// fb_small_kernel: the same E step for J <= 32 states, with each step's
+// serial chain cut short.  Per forward step: warp 0 (a lane per state) forms
+// the normaliser N[t] with one shuffle reduction and the ratios r = pdf / N;
+// a warp per state updates its product ring and sums F[j][t] over u with the
+// window of StateIn kept in shared memory; a warp per state then forms
+// StateIn[j][t+1] and the eta weight A[j][t] = sum_{i != j} p[i][j] F[i][t]
+// with lanes over i.  The ratios and weights are kept for the backward pass,
+// which needs no division or transition sum on its chain: the segment terms
+// are (ob * d[j][u]) * q[j][e] with q = L1 / F formed once per (j, e) and kept
+// in a ring, and L1 takes one shuffle reduction over k.  The sums over i, k
+// and j associate as trees here (the reference sums them in order), which
+// moves results by rounding only.
+__global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
+  extern __shared__ __align__(16) unsigned char fsm[];
+  const int J = a.J, M = a.M, tau = a.tau;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const bool right = a.censoring == 1;
+  double* rings = a.rings_in_smem ? (double*)fsm : a.ring;
+  double* Pf = rings;                          // [J][M] forward products, by segment start % M
+  double* Pb = Pf + (size_t)J * M;             // [J][M] backward products, by segment end % M
+  double* Sr = Pb + (size_t)J * M;             // [J][M] StateIn window, by step % M
+  double* Qr = Sr + (size_t)J * M;             // [J][M] L1 / F window, by step % M
+  __shared__ double s_r[32], s_F[32], s_S[32], s_G[32];
+  __shared__ int s_bad;
+  auto at = [&](double* x, int j, long long t) -> double& { return x[(size_t)j * tau + t]; };
+  auto atc = [&](const double* x, int j, long long t) -> double { return x[(size_t)j * tau + t]; };
+  auto dd = [&](int j, int u) -> double { return a.d[(size_t)j * M + (u - 1)]; };
+  auto DD = [&](int j, int u) -> double { return u <= M ? a.D[(size_t)j * (M + 1) + u] : 0.0; };
+  auto pp = [&](int i, int j) -> double { return a.p[(size_t)i * J + j]; };
+
+  if (tid == 0) s_bad = 0;
+  for (int j = warp; j < J; j += nw)
+    for (int u = lane + 1; u <= M; u += 32) {
+      double x = 0;
+      for (int v = u; v <= M; ++v) x += dd(j, v);
+      a.D[(size_t)j * (M + 1) + u] = x;
+      a.eta[(size_t)j * M + (u - 1)] = 0.0;
+    }
+  __syncthreads();
+
+  // ---- forward ----
+  double Fprev = 0.0, Nmprev = 0.0, Scur = 0.0;  // warp 0, lane j: F[j][t-1], Norm[j][t-1], StateIn[j][t]
+  for (int t = 0; t < tau; ++t) {
+    if (warp == 0) {
+      const bool has = lane < J;
+      double raw = 0.0;
+      if (has) raw = t == 0 ? atc(a.pdf, lane, 0) * a.pi[lane] : atc(a.pdf, lane, t) * (Scur - Fprev + Nmprev);
+      const double n = warp_sum(raw);
+      if (has) {
+        const double nm = raw / n;
+        at(a.Norm, lane, t) = nm;
+        Nmprev = nm;
+        const double r = atc(a.pdf, lane, t) / n;
+        s_r[lane] = r;
+        at(a.R, lane, t) = r;
+      }
+      if (lane == 0) {
+        a.N[t] = n;
+        if (!(n > 0)) s_bad = 1;
+      }
+    }
+    __syncthreads();
+    if (s_bad) break;
+    const bool last = t == tau - 1;
+    const int umax = min(t + 1, M);
+    for (int j = warp; j < J; j += nw) {
+      const double r = s_r[j];
+      double* P = Pf + (size_t)j * M;
+      const double* Sj = Sr + (size_t)j * M;
+      double part = 0.0;
+      for (int u = lane + 1; u <= umax; u += 32) {
+        const int s = t - u + 1;
+        const int slot = s % M;
+        const double ob = (u == 1) ? r : P[slot] * r;
+        P[slot] = ob;
+        const double du = last ? DD(j, u) : dd(j, u);
+        part += (s > 0) ? ob * du * Sj[slot] : ob * du * a.pi[j];
+      }
+      const double f = warp_sum(part);
+      if (lane == 0) {
+        s_F[j] = f;
+        at(a.F, j, t) = f;
+        if (!(f > 0)) s_bad = 1;
+      }
+    }
+    __syncthreads();
+    if (s_bad) break;
+    if (t < tau - 1)
+      for (int j = warp; j < J; j += nw) {
+        const double pr = lane < J ? pp(lane, j) * s_F[lane] : 0.0;
+        const double sv = warp_sum(pr);
+        const double av = warp_sum(lane != j ? pr : 0.0);
+        if (lane == 0) {
+          Sr[(size_t)j * M + (t + 1) % M] = sv;
+          s_S[j] = sv;
+          at(a.S, j, t + 1) = sv;
+          at(a.A, j, t) = av;
+        }
+      }
+    __syncthreads();
+    if (warp == 0 && lane < J) {
+      Fprev = s_F[lane];
+      Scur = s_S[lane];
+    }
+  }
+  if (s_bad) {
+    if (tid == 0) *a.status = 1;
+    return;
+  }
+
+  // ---- backward ----
+  for (int j = warp; j < J; j += nw)
+    if (lane == 0) at(a.L, j, tau - 1) = at(a.F, j, tau - 1);
+  __syncthreads();
+  for (int t = tau - 2; t >= 0; --t) {
+    const int span = tau - 1 - t;
+    const int umax = min(span, M);
+    for (int j = warp; j < J; j += nw) {
+      const double r = at(a.R, j, t + 1);
+      const double A = at(a.A, j, t);
+      double* Q = Pb + (size_t)j * M;
+      const double* qj = Qr + (size_t)j * M;
+      double part = 0.0;
+      for (int u = lane + 1; u <= umax; u += 32) {
+        const int e = t + u;
+        const int slot = e % M;
+        const double ob = (u == 1) ? r : Q[slot] * r;
+        Q[slot] = ob;
+        const double h = (u < span) ? (ob * dd(j, u)) * qj[slot] : ob * DD(j, span);
+        part += h;
+        if (u <= span - 1) a.eta[(size_t)j * M + (u - 1)] += A * h;
+      }
+      if (right && span <= M) {
+        __syncwarp();
+        const double s_t = Q[(tau - 1) % M];
+        for (int u = lane + 1; u <= M; u += 32)
+          if (u >= span) a.eta[(size_t)j * M + (u - 1)] += A * (s_t * dd(j, u));
+      }
+      const double g = warp_sum(part);
+      if (lane == 0) {
+        s_G[j] = g;
+        at(a.G, j, t + 1) = g;
+      }
+    }
+    __syncthreads();
+    for (int j = warp; j < J; j += nw) {
+      const double gv = lane < J ? s_G[lane] * pp(j, lane) : 0.0;
+      const double sum = warp_sum(gv);
+      if (lane == 0) {
+        const double f = at(a.F, j, t);
+        const double l1 = sum * f;
+        at(a.L1, j, t) = l1;
+        at(a.L, j, t) = l1 + at(a.L, j, t + 1) - s_G[j] * at(a.S, j, t + 1);
+        Qr[(size_t)j * M + t % M] = l1 / f;
+      }
+    }
+    __syncthreads();
+  }
+
   for (int j = warp; j < J; j += nw)
     for (int u = lane + 1; u <= M; u += 32) {
       if (!(right || u <= tau - 1)) continue;

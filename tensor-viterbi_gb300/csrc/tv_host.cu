@@ -928,9 +928,15 @@ int fb_run(int censoring, int64_t tau, int J, int M, const double* d, const doub
   int dev = 0, smem_optin = 0;
   TV_CUDA(cudaGetDevice(&dev));
   TV_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  const size_t ring_bytes = 2 * JM * sizeof(double);
-  const bool in_smem = ring_bytes + 1024 <= (size_t)smem_optin;
-  if (!in_smem && b.get(&dring, 2 * JM)) return fail(TV_ENOMEM, "tv_fb: device allocation failed");
+  // J <= 32: the short-chain kernel (four rings, the ratios and eta weights
+  // kept for the backward pass); otherwise the general one
+  const bool small = J <= 32;
+  const size_t nrings = small ? 4 : 2;
+  const size_t ring_bytes = nrings * JM * sizeof(double);
+  const bool in_smem = ring_bytes + 2048 <= (size_t)smem_optin;
+  if (!in_smem && b.get(&dring, nrings * JM)) return fail(TV_ENOMEM, "tv_fb: device allocation failed");
+  double *dR = nullptr, *dA = nullptr;
+  if (small && (b.get(&dR, JT) || b.get(&dA, JT))) return fail(TV_ENOMEM, "tv_fb: device allocation failed");
   TV_CUDA(cudaMemcpy(dd, d, sizeof(double) * JM, cudaMemcpyHostToDevice));
   TV_CUDA(cudaMemcpy(dp, p, sizeof(double) * J * J, cudaMemcpyHostToDevice));
   TV_CUDA(cudaMemcpy(dpi, pi, sizeof(double) * J, cudaMemcpyHostToDevice));
@@ -945,13 +951,16 @@ int fb_run(int censoring, int64_t tau, int J, int M, const double* d, const doub
   A.d = dd; A.p = dp; A.pi = dpi; A.pdf = dpdf;
   A.F = dF; A.L = dL; A.G = dG; A.L1 = dL1; A.N = dN; A.Norm = dNorm; A.eta = deta;
   A.S = dS; A.D = dD; A.ring = dring; A.rings_in_smem = in_smem ? 1 : 0; A.status = dst;
+  A.R = dR; A.A = dA;
   const int threads = 32 * std::min(32, J);
   const size_t dyn = in_smem ? ring_bytes : 0;
+  const void* kern = small ? (const void*)tv::fb_small_kernel : (const void*)tv::fb_kernel;
   if (dyn) {
-    int rc = raise_smem_limit((const void*)tv::fb_kernel);
+    int rc = raise_smem_limit(kern);
     if (rc != TV_OK) return rc;
   }
-  tv::fb_kernel<<<1, threads, dyn>>>(A);
+  if (small) tv::fb_small_kernel<<<1, threads, dyn>>>(A);
+  else tv::fb_kernel<<<1, threads, dyn>>>(A);
   TV_CUDA(cudaGetLastError());
   int st = 0;
   TV_CUDA(cudaMemcpy(&st, dst, sizeof(int), cudaMemcpyDeviceToHost));
