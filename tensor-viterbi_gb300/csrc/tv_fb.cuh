@@ -237,18 +237,22 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
   __syncthreads();
 
   // ---- forward ----
+  // Values read from global memory on a step's chain are loaded one step
+  // ahead into registers (a global load costs hundreds of clocks).
   double Fprev = 0.0, Nmprev = 0.0, Scur = 0.0;  // warp 0, lane j: F[j][t-1], Norm[j][t-1], StateIn[j][t]
+  double pdf_cur = (warp == 0 && lane < J) ? atc(a.pdf, lane, 0) : 0.0;
   for (int t = 0; t < tau; ++t) {
     if (warp == 0) {
       const bool has = lane < J;
+      const double pdf_nx = (has && t + 1 < tau) ? atc(a.pdf, lane, t + 1) : 0.0;
       double raw = 0.0;
-      if (has) raw = t == 0 ? atc(a.pdf, lane, 0) * a.pi[lane] : atc(a.pdf, lane, t) * (Scur - Fprev + Nmprev);
+      if (has) raw = t == 0 ? pdf_cur * a.pi[lane] : pdf_cur * (Scur - Fprev + Nmprev);
       const double n = warp_sum(raw);
       if (has) {
         const double nm = raw / n;
         at(a.Norm, lane, t) = nm;
         Nmprev = nm;
-        const double r = atc(a.pdf, lane, t) / n;
+        const double r = pdf_cur / n;
         s_r[lane] = r;
         at(a.R, lane, t) = r;
       }
@@ -256,6 +260,7 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
         a.N[t] = n;
         if (!(n > 0)) s_bad = 1;
       }
+      pdf_cur = pdf_nx;
     }
     __syncthreads();
     if (s_bad) break;
@@ -307,15 +312,34 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
   }
 
   // ---- backward ----
-  for (int j = warp; j < J; j += nw)
-    if (lane == 0) at(a.L, j, tau - 1) = at(a.F, j, tau - 1);
+  // warp j (one state per warp here): the values of step t, loaded during
+  // step t+1, and L[j][t+1] from the previous step
+  const int jw = warp;  // nw == J
+  double Lnext = 0.0, r_nx = 0.0, A_nx = 0.0, f_nx = 0.0, s_nx = 0.0;
+  if (jw < J) {
+    Lnext = at(a.F, jw, tau - 1);
+    if (lane == 0) at(a.L, jw, tau - 1) = Lnext;
+    if (tau >= 2) {
+      r_nx = at(a.R, jw, tau - 1);
+      A_nx = at(a.A, jw, tau - 2);
+      f_nx = at(a.F, jw, tau - 2);
+      s_nx = at(a.S, jw, tau - 1);
+    }
+  }
   __syncthreads();
   for (int t = tau - 2; t >= 0; --t) {
     const int span = tau - 1 - t;
     const int umax = min(span, M);
+    const double r_t = r_nx, A_t = A_nx, f_t = f_nx, s_t1 = s_nx;
+    if (jw < J && t >= 1) {
+      r_nx = at(a.R, jw, t);
+      A_nx = at(a.A, jw, t - 1);
+      f_nx = at(a.F, jw, t - 1);
+      s_nx = at(a.S, jw, t);
+    }
     for (int j = warp; j < J; j += nw) {
-      const double r = at(a.R, j, t + 1);
-      const double A = at(a.A, j, t);
+      const double r = r_t;
+      const double A = A_t;
       double* Q = Pb + (size_t)j * M;
       const double* qj = Qr + (size_t)j * M;
       double part = 0.0;
@@ -345,10 +369,12 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
       const double gv = lane < J ? s_G[lane] * pp(j, lane) : 0.0;
       const double sum = warp_sum(gv);
       if (lane == 0) {
-        const double f = at(a.F, j, t);
+        const double f = f_t;
         const double l1 = sum * f;
         at(a.L1, j, t) = l1;
-        at(a.L, j, t) = l1 + at(a.L, j, t + 1) - s_G[j] * at(a.S, j, t + 1);
+        const double lv = l1 + Lnext - s_G[j] * s_t1;
+        at(a.L, j, t) = lv;
+        Lnext = lv;
         Qr[(size_t)j * M + t % M] = l1 / f;
       }
     }
