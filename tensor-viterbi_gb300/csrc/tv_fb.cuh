@@ -218,11 +218,15 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
   double* Pb = Pf + (size_t)J * M;             // [J][M] backward products, by segment end % M
   double* Sr = Pb + (size_t)J * M;             // [J][M] StateIn window, by step % M
   double* Qr = Sr + (size_t)J * M;             // [J][M] L1 / F window, by step % M
+  // eta accumulators: in shared memory with the rings (a global
+  // read-modify-write per duration and step would put the L2 latency on the
+  // backward chain), copied out at the end
+  double* Et = a.rings_in_smem ? Qr + (size_t)J * M : a.eta;
   __shared__ double s_r[32], s_F[32], s_S[32], s_G[32];
   __shared__ int s_bad;
   auto at = [&](double* x, int j, long long t) -> double& { return x[(size_t)j * tau + t]; };
   auto atc = [&](const double* x, int j, long long t) -> double { return x[(size_t)j * tau + t]; };
-  auto dd = [&](int j, int u) -> double { return a.d[(size_t)j * M + (u - 1)]; };
+  auto dd = [&](int j, int u) -> double { return __ldg(a.d + (size_t)j * M + (u - 1)); };
   auto DD = [&](int j, int u) -> double { return u <= M ? a.D[(size_t)j * (M + 1) + u] : 0.0; };
   auto pp = [&](int i, int j) -> double { return a.p[(size_t)i * J + j]; };
 
@@ -232,7 +236,7 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
       double x = 0;
       for (int v = u; v <= M; ++v) x += dd(j, v);
       a.D[(size_t)j * (M + 1) + u] = x;
-      a.eta[(size_t)j * M + (u - 1)] = 0.0;
+      Et[(size_t)j * M + (u - 1)] = 0.0;
     }
   __syncthreads();
 
@@ -350,13 +354,13 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
         Q[slot] = ob;
         const double h = (u < span) ? (ob * dd(j, u)) * qj[slot] : ob * DD(j, span);
         part += h;
-        if (u <= span - 1) a.eta[(size_t)j * M + (u - 1)] += A * h;
+        if (u <= span - 1) Et[(size_t)j * M + (u - 1)] += A * h;
       }
       if (right && span <= M) {
         __syncwarp();
         const double s_t = Q[(tau - 1) % M];
         for (int u = lane + 1; u <= M; u += 32)
-          if (u >= span) a.eta[(size_t)j * M + (u - 1)] += A * (s_t * dd(j, u));
+          if (u >= span) Et[(size_t)j * M + (u - 1)] += A * (s_t * dd(j, u));
       }
       const double g = warp_sum(part);
       if (lane == 0) {
@@ -391,8 +395,13 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
       } else {
         for (int v = 1; v <= tau; ++v) r *= atc(a.pdf, j, tau - v) / a.N[tau - v];
       }
-      a.eta[(size_t)j * M + (u - 1)] += r;
+      Et[(size_t)j * M + (u - 1)] += r;
     }
+  if (a.rings_in_smem) {
+    __syncwarp();
+    for (int j = warp; j < J; j += nw)
+      for (int u = lane + 1; u <= M; u += 32) a.eta[(size_t)j * M + (u - 1)] = Et[(size_t)j * M + (u - 1)];
+  }
   if (tid == 0) *a.status = 0;
 }
 

@@ -932,7 +932,7 @@ int fb_run(int censoring, int64_t tau, int J, int M, const double* d, const doub
   // kept for the backward pass); otherwise the general one
   const bool small = J <= 32;
   const size_t nrings = small ? 4 : 2;
-  const size_t ring_bytes = nrings * JM * sizeof(double);
+  const size_t ring_bytes = (nrings + (small ? 1 : 0)) * JM * sizeof(double);  // + eta accumulators
   const bool in_smem = ring_bytes + 2048 <= (size_t)smem_optin;
   if (!in_smem && b.get(&dring, nrings * JM)) return fail(TV_ENOMEM, "tv_fb: device allocation failed");
   double *dR = nullptr, *dA = nullptr;
