@@ -196,39 +196,51 @@ __global__ void __launch_bounds__(1024) fb_kernel(FbArgs a) {
   if (tid == 0) *a.status = 0;
 }
 
-// fb_small_kernel: the same E step for J <= 32 states, with each step's
-// serial chain cut short.  Per forward step: warp 0 (a lane per state) forms
-// the normaliser N[t] with one shuffle reduction and the ratios r = pdf / N;
-// a warp per state updates its product ring and sums F[j][t] over u with the
-// window of StateIn kept in shared memory; a warp per state then forms
-// StateIn[j][t+1] and the eta weight A[j][t] = sum_{i != j} p[i][j] F[i][t]
-// with lanes over i.  The ratios and weights are kept for the backward pass,
-// which needs no division or transition sum on its chain: the segment terms
-// are (ob * d[j][u]) * q[j][e] with q = L1 / F formed once per (j, e) and kept
-// in a ring, and L1 takes one shuffle reduction over k.  The sums over i, k
-// and j associate as trees here (the reference sums them in order), which
-// moves results by rounding only.
+// fb_small_kernel: the same E step for J <= 32 states, written for GB300's
+// FP64 units, which take one warp instruction per 64 clocks per
+// sub-partition whatever the number of active lanes: the cost of a step is
+// its count of FP64 warp instructions, so the work is packed into few of them.
+//   forward:  warp 0 (a lane per state) forms the normaliser N[t] with one
+//             shuffle reduction and one division, then the ratios
+//             r = pdf * (1/N); a warp per state keeps W(s) = P(s..t) * StateIn(s)
+//             for the segment starts s of the window (one multiply by r per
+//             entry and step) and sums F = sum_u W(s) * dur(u); groups of
+//             lanes (a power of two >= J per state) form StateIn[j][t+1] and
+//             the eta weight A[j][t] = sum_{i != j} p[i][j] F[i][t].
+//   backward: a warp per state keeps V(e) = Q(t+1..e) * L1(e) / F(e) for the
+//             segment ends e, so a segment term is V(e) * d(u); the
+//             right-censoring product s is formed in the reference's order;
+//             groups of lanes form L1 = F * sum_k G[k] p[j][k] and L.
+// The ratios and weights of the forward pass are kept for the backward pass.
+// Products, the sums over u, i, k and j and the divisions associate
+// differently from the reference (which sums in order and divides each
+// term), which moves results by rounding only.
 __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
   extern __shared__ __align__(16) unsigned char fsm[];
   const int J = a.J, M = a.M, tau = a.tau;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   const bool right = a.censoring == 1;
   double* rings = a.rings_in_smem ? (double*)fsm : a.ring;
-  double* Pf = rings;                          // [J][M] forward products, by segment start % M
-  double* Pb = Pf + (size_t)J * M;             // [J][M] backward products, by segment end % M
-  double* Sr = Pb + (size_t)J * M;             // [J][M] StateIn window, by step % M
-  double* Qr = Sr + (size_t)J * M;             // [J][M] L1 / F window, by step % M
+  double* Wf = rings;                          // [J][M] forward W, by segment start % M
+  double* Vb = Wf + (size_t)J * M;             // [J][M] backward V, by segment end % M
   // eta accumulators: in shared memory with the rings (a global
   // read-modify-write per duration and step would put the L2 latency on the
   // backward chain), copied out at the end
-  double* Et = a.rings_in_smem ? Qr + (size_t)J * M : a.eta;
-  __shared__ double s_r[32], s_F[32], s_S[32], s_G[32];
+  double* Et = a.rings_in_smem ? Vb + (size_t)J * M : a.eta;
+  __shared__ double s_r[32], s_F[32], s_S[32], s_G[32], s_q[32];
   __shared__ int s_bad;
   auto at = [&](double* x, int j, long long t) -> double& { return x[(size_t)j * tau + t]; };
   auto atc = [&](const double* x, int j, long long t) -> double { return x[(size_t)j * tau + t]; };
   auto dd = [&](int j, int u) -> double { return __ldg(a.d + (size_t)j * M + (u - 1)); };
   auto DD = [&](int j, int u) -> double { return u <= M ? a.D[(size_t)j * (M + 1) + u] : 0.0; };
-  auto pp = [&](int i, int j) -> double { return a.p[(size_t)i * J + j]; };
+  auto pp = [&](int i, int j) -> double { return __ldg(a.p + (size_t)i * J + j); };
+  // lane groups for the J x J sums: Gs lanes per state, 32 / Gs states a warp
+  int Gs = 1;
+  while (Gs < J) Gs <<= 1;
+  const int per_warp = 32 / Gs;
+  const int gj = warp * per_warp + lane / Gs;  // this lane's state in the grouped sums
+  const int gi = lane % Gs;                     // and its i (or k)
+  const bool glead = gi == 0 && gj < J;
 
   if (tid == 0) s_bad = 0;
   for (int j = warp; j < J; j += nw)
@@ -238,6 +250,7 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
       a.D[(size_t)j * (M + 1) + u] = x;
       Et[(size_t)j * M + (u - 1)] = 0.0;
     }
+  if (tid < 32) s_S[tid] = 0.0;
   __syncthreads();
 
   // ---- forward ----
@@ -252,11 +265,12 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
       double raw = 0.0;
       if (has) raw = t == 0 ? pdf_cur * a.pi[lane] : pdf_cur * (Scur - Fprev + Nmprev);
       const double n = warp_sum(raw);
+      const double inv = 1.0 / n;
       if (has) {
-        const double nm = raw / n;
+        const double nm = raw * inv;
         at(a.Norm, lane, t) = nm;
         Nmprev = nm;
-        const double r = pdf_cur / n;
+        const double r = pdf_cur * inv;
         s_r[lane] = r;
         at(a.R, lane, t) = r;
       }
@@ -272,16 +286,15 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
     const int umax = min(t + 1, M);
     for (int j = warp; j < J; j += nw) {
       const double r = s_r[j];
-      double* P = Pf + (size_t)j * M;
-      const double* Sj = Sr + (size_t)j * M;
+      double* W = Wf + (size_t)j * M;
       double part = 0.0;
       for (int u = lane + 1; u <= umax; u += 32) {
         const int s = t - u + 1;
         const int slot = s % M;
-        const double ob = (u == 1) ? r : P[slot] * r;
-        P[slot] = ob;
-        const double du = last ? DD(j, u) : dd(j, u);
-        part += (s > 0) ? ob * du * Sj[slot] : ob * du * a.pi[j];
+        // a new segment start takes StateIn (or pi for s = 0) once
+        const double w = (u == 1) ? r * (t > 0 ? s_S[j] : a.pi[j]) : W[slot] * r;
+        W[slot] = w;
+        part += w * (last ? DD(j, u) : dd(j, u));
       }
       const double f = warp_sum(part);
       if (lane == 0) {
@@ -292,18 +305,19 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
     }
     __syncthreads();
     if (s_bad) break;
-    if (t < tau - 1)
-      for (int j = warp; j < J; j += nw) {
-        const double pr = lane < J ? pp(lane, j) * s_F[lane] : 0.0;
-        const double sv = warp_sum(pr);
-        const double av = warp_sum(lane != j ? pr : 0.0);
-        if (lane == 0) {
-          Sr[(size_t)j * M + (t + 1) % M] = sv;
-          s_S[j] = sv;
-          at(a.S, j, t + 1) = sv;
-          at(a.A, j, t) = av;
-        }
+    if (t < tau - 1 && warp * per_warp < J) {
+      const double pr = (gj < J && gi < J) ? pp(gi, gj) * s_F[gi] : 0.0;
+      double sv = pr, av = gi != gj ? pr : 0.0;
+      for (int o = Gs >> 1; o > 0; o >>= 1) {
+        sv += __shfl_xor_sync(0xffffffffu, sv, o);
+        av += __shfl_xor_sync(0xffffffffu, av, o);
       }
+      if (glead) {
+        s_S[gj] = sv;
+        at(a.S, gj, t + 1) = sv;
+        at(a.A, gj, t) = av;
+      }
+    }
     __syncthreads();
     if (warp == 0 && lane < J) {
       Fprev = s_F[lane];
@@ -316,52 +330,55 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
   }
 
   // ---- backward ----
-  // warp j (one state per warp here): the values of step t, loaded during
-  // step t+1, and L[j][t+1] from the previous step
+  // warp j (a warp per state): r = pdf/N of step t+1 and the eta weight of
+  // step t, loaded during step t+1; the group leader of state j: F[j][t],
+  // StateIn[j][t+1] likewise, and L[j][t+1] from the previous step
   const int jw = warp;  // nw == J
-  double Lnext = 0.0, r_nx = 0.0, A_nx = 0.0, f_nx = 0.0, s_nx = 0.0;
-  if (jw < J) {
-    Lnext = at(a.F, jw, tau - 1);
-    if (lane == 0) at(a.L, jw, tau - 1) = Lnext;
+  double r_nx = 0.0, A_nx = 0.0, s_tail = 1.0;
+  if (jw < J && tau >= 2) {
+    r_nx = at(a.R, jw, tau - 1);
+    A_nx = at(a.A, jw, tau - 2);
+  }
+  double Lnext = 0.0, f_nx = 0.0, st_nx = 0.0;
+  if (glead) {
+    Lnext = at(a.F, gj, tau - 1);
+    at(a.L, gj, tau - 1) = Lnext;
     if (tau >= 2) {
-      r_nx = at(a.R, jw, tau - 1);
-      A_nx = at(a.A, jw, tau - 2);
-      f_nx = at(a.F, jw, tau - 2);
-      s_nx = at(a.S, jw, tau - 1);
+      f_nx = at(a.F, gj, tau - 2);
+      st_nx = at(a.S, gj, tau - 1);
     }
   }
   __syncthreads();
   for (int t = tau - 2; t >= 0; --t) {
     const int span = tau - 1 - t;
     const int umax = min(span, M);
-    const double r_t = r_nx, A_t = A_nx, f_t = f_nx, s_t1 = s_nx;
+    const double r = r_nx, A = A_nx;
     if (jw < J && t >= 1) {
       r_nx = at(a.R, jw, t);
       A_nx = at(a.A, jw, t - 1);
-      f_nx = at(a.F, jw, t - 1);
-      s_nx = at(a.S, jw, t);
     }
-    for (int j = warp; j < J; j += nw) {
-      const double r = r_t;
-      const double A = A_t;
-      double* Q = Pb + (size_t)j * M;
-      const double* qj = Qr + (size_t)j * M;
+    if (jw < J) {
+      const int j = jw;
+      s_tail = s_tail * r;  // the reference's s: r[tau-1] * r[tau-2] * ... * r[t+1]
+      double* V = Vb + (size_t)j * M;
       double part = 0.0;
       for (int u = lane + 1; u <= umax; u += 32) {
         const int e = t + u;
-        const int slot = e % M;
-        const double ob = (u == 1) ? r : Q[slot] * r;
-        Q[slot] = ob;
-        const double h = (u < span) ? (ob * dd(j, u)) * qj[slot] : ob * DD(j, span);
+        double h;
+        if (u < span) {
+          const int slot = e % M;
+          const double v = (u == 1) ? r * s_q[j] : V[slot] * r;  // s_q[j] = L1(t+1) / F(t+1)
+          V[slot] = v;
+          h = v * dd(j, u);
+          Et[(size_t)j * M + (u - 1)] += A * h;
+        } else {
+          h = s_tail * DD(j, span);
+        }
         part += h;
-        if (u <= span - 1) Et[(size_t)j * M + (u - 1)] += A * h;
       }
-      if (right && span <= M) {
-        __syncwarp();
-        const double s_t = Q[(tau - 1) % M];
+      if (right && span <= M)
         for (int u = lane + 1; u <= M; u += 32)
-          if (u >= span) Et[(size_t)j * M + (u - 1)] += A * (s_t * dd(j, u));
-      }
+          if (u >= span) Et[(size_t)j * M + (u - 1)] += A * (s_tail * dd(j, u));
       const double g = warp_sum(part);
       if (lane == 0) {
         s_G[j] = g;
@@ -369,22 +386,27 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
       }
     }
     __syncthreads();
-    for (int j = warp; j < J; j += nw) {
-      const double gv = lane < J ? s_G[lane] * pp(j, lane) : 0.0;
-      const double sum = warp_sum(gv);
-      if (lane == 0) {
-        const double f = f_t;
-        const double l1 = sum * f;
-        at(a.L1, j, t) = l1;
-        const double lv = l1 + Lnext - s_G[j] * s_t1;
-        at(a.L, j, t) = lv;
+    const double f_t = f_nx, st1 = st_nx;
+    if (glead && t >= 1) {
+      f_nx = at(a.F, gj, t - 1);
+      st_nx = at(a.S, gj, t);
+    }
+    if (warp * per_warp < J) {
+      double sv = (gj < J && gi < J) ? s_G[gi] * pp(gj, gi) : 0.0;
+      for (int o = Gs >> 1; o > 0; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o);
+      if (glead) {
+        const double l1 = sv * f_t;
+        at(a.L1, gj, t) = l1;
+        const double lv = l1 + Lnext - s_G[gj] * st1;
+        at(a.L, gj, t) = lv;
         Lnext = lv;
-        Qr[(size_t)j * M + t % M] = l1 / f;
+        s_q[gj] = l1 / f_t;
       }
     }
     __syncthreads();
   }
 
+  // eta: the segment that starts at t = 0 (FBImpl.cpp:252-266)
   for (int j = warp; j < J; j += nw)
     for (int u = lane + 1; u <= M; u += 32) {
       if (!(right || u <= tau - 1)) continue;
@@ -398,7 +420,7 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
       Et[(size_t)j * M + (u - 1)] += r;
     }
   if (a.rings_in_smem) {
-    __syncwarp();
+    __syncthreads();
     for (int j = warp; j < J; j += nw)
       for (int u = lane + 1; u <= M; u += 32) a.eta[(size_t)j * M + (u - 1)] = Et[(size_t)j * M + (u - 1)];
   }

@@ -928,11 +928,12 @@ int fb_run(int censoring, int64_t tau, int J, int M, const double* d, const doub
   int dev = 0, smem_optin = 0;
   TV_CUDA(cudaGetDevice(&dev));
   TV_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  // J <= 32: the short-chain kernel (four rings, the ratios and eta weights
-  // kept for the backward pass); otherwise the general one
+  // J <= 32: the short-chain kernel (a forward and a backward ring, the
+  // ratios and eta weights kept for the backward pass); otherwise the
+  // general one
   const bool small = J <= 32;
-  const size_t nrings = small ? 4 : 2;
-  const size_t ring_bytes = (nrings + (small ? 1 : 0)) * JM * sizeof(double);  // + eta accumulators
+  const size_t nrings = small ? 3 : 2;  // small: forward and backward rings + eta accumulators
+  const size_t ring_bytes = nrings * JM * sizeof(double);
   const bool in_smem = ring_bytes + 2048 <= (size_t)smem_optin;
   if (!in_smem && b.get(&dring, nrings * JM)) return fail(TV_ENOMEM, "tv_fb: device allocation failed");
   double *dR = nullptr, *dA = nullptr;
