@@ -4,22 +4,23 @@
 // (hsmmlearn/hsmmlearn/hsmm.py:181-305), whose E step is FBImpl
 // (hsmmlearn/hsmmlearn/_hsmm/src/FBImpl.cpp): Guedon's scaled forward and
 // backward recursions for an explicit-duration HSMM, then the expected
-// duration counts eta.  This kernel computes the same arrays with the same
-// formulas; one CTA runs one sequence, a warp per state (lanes over the
-// durations u) for the O(J*M) sums of a step, a thread per state for the
-// O(J) normalisation and transition sums, which keep the reference's
-// sequential order (j, i or k ascending).
+// duration counts eta.  These kernels compute the same arrays with the same
+// formulas; one CTA runs one sequence.  fb_kernel (any J) uses a warp per
+// state (lanes over the durations u) for the O(J*M) sums of a step and a
+// thread per state for the O(J) normalisation and transition sums, which
+// keep the reference's sequential order (j, i or k ascending);
+// fb_small_kernel (J <= 32) shortens the chain of a step (below).
 //
 // The products of likelihood ratios r_s = pdf[j][s] / N[s] over a segment
-// are kept in a ring per state, indexed by the segment's first (forward) or
-// last (backward) step, and multiplied by the new ratio every step (one
-// multiply per cell, like the decoder's window folds), instead of being
-// rebuilt for every u as the reference does; and the sums over u are lane
-// partials reduced by shuffles.  Both change the association of some
-// products and sums, so results agree with the reference to rounding
-// (relative differences of order 1e-14 on the tests' sequences), not bit for
-// bit.  The eta sums keep the reference's order over t, and the backward
-// right-censoring product s is formed in the reference's order.
+// are kept per state and duration (in a ring indexed by the segment's first
+// (forward) or last (backward) step, or in registers), and multiplied by the
+// new ratio every step (one multiply per cell, like the decoder's window
+// folds), instead of being rebuilt for every u as the reference does; and
+// the sums over u are lane partials reduced by shuffles.  Both change the
+// association of some products and sums, so results agree with the
+// reference to rounding (relative differences of order 1e-13 on the tests'
+// sequences), not bit for bit.  The backward right-censoring product s is
+// formed in the reference's order.
 //
 // Censoring 0 (none) and 1 (right censoring, the fit's default) are
 // supported; the reference's left-censoring variant (2) is not.
@@ -39,7 +40,7 @@ struct FbArgs {
   double* S;          // (J, tau) scratch: StateIn
   double* D;          // (J, M+1) scratch: survival D[j][u] = sum_{v >= u} d[j][v]
   double* ring;       // (2, J, M) scratch when the rings do not fit shared memory
-                      // (fb_small_kernel: (4, J, M))
+                      // (fb_small_kernel: the first two of (3, J, M))
   int rings_in_smem;
   double* R;          // (J, tau) scratch of fb_small_kernel: r = pdf / N
   double* A;          // (J, tau) scratch of fb_small_kernel: sum_{i != j} p[i][j] F[i][t]
@@ -196,36 +197,55 @@ __global__ void __launch_bounds__(1024) fb_kernel(FbArgs a) {
   if (tid == 0) *a.status = 0;
 }
 
-// fb_small_kernel: the same E step for J <= 32 states, written for GB300's
-// FP64 units, which take one warp instruction per 64 clocks per
-// sub-partition whatever the number of active lanes: the cost of a step is
-// its count of FP64 warp instructions, so the work is packed into few of them.
+// Sum over the aligned group of g lanes (g a power of two <= 32); every lane
+// of the warp takes part.
+__device__ __forceinline__ double group_sum(double v, int g) {
+  for (int o = g >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Durations a lane of fb_small_kernel<K> holds in registers: u = lane + 1 + 32k
+// for k < K, so K = ceil(M / 32) blocks cover the window.
+constexpr int FB_REG_BLOCKS = 4;
+
+// fb_small_kernel: the same E step for J <= 32 states, one warp per state.
+// A step is a chain of dependent FP64 operations, shuffles and barriers on
+// one SM (a sequence has no other parallelism), and GB300's FP64 units have
+// a long dependent latency, so the kernel keeps that chain short:
 //   forward:  warp 0 (a lane per state) forms the normaliser N[t] with one
 //             shuffle reduction and one division, then the ratios
-//             r = pdf * (1/N); a warp per state keeps W(s) = P(s..t) * StateIn(s)
-//             for the segment starts s of the window (one multiply by r per
-//             entry and step) and sums F = sum_u W(s) * dur(u); groups of
-//             lanes (a power of two >= J per state) form StateIn[j][t+1] and
-//             the eta weight A[j][t] = sum_{i != j} p[i][j] F[i][t].
-//   backward: a warp per state keeps V(e) = Q(t+1..e) * L1(e) / F(e) for the
-//             segment ends e, so a segment term is V(e) * d(u); the
+//             r = pdf * (1/N); warp j keeps, per duration u of the window,
+//             W(u) = P(t-u+1..t) * StateIn(t-u+1) (the segment that starts at
+//             t-u+1), which is W(u-1) of step t-1 times r: with K > 0 the
+//             entries live in registers (lane + 32k holds u = lane + 1 + 32k)
+//             and move up one duration per step by warp shuffles; with K = 0
+//             in a shared-memory ring indexed by the segment start.  F is the
+//             sum of W(u) * dur(u), fused multiply-adds and a warp reduction;
+//             groups of lanes (a power of two >= J per state) form
+//             StateIn[j][t+1] and the eta weight A[j][t] = sum_{i != j} p[i][j] F[i][t].
+//   backward: warp j keeps V(u) = Q(t+1..t+u) * L1(t+u) / F(t+u) for the
+//             segment that ends at t+u, V(u-1) of step t+1 times r, the same
+//             way, so a segment term is V(u) * d(u); the eta accumulators take
+//             A * V without the factor d(u), applied once at the end; the
 //             right-censoring product s is formed in the reference's order;
-//             groups of lanes form L1 = F * sum_k G[k] p[j][k] and L.
+//             groups of lanes form L1 = F * sum_k G[k] p[j][k] and L, and
+//             L1 / F is taken as that sum.
 // The ratios and weights of the forward pass are kept for the backward pass.
-// Products, the sums over u, i, k and j and the divisions associate
-// differently from the reference (which sums in order and divides each
-// term), which moves results by rounding only.
+// Products, the sums over u, i, k and j, fused multiply-adds and the
+// divisions associate differently from the reference (which sums in order
+// and divides each term), which moves results by rounding only.
+template <int K>
 __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
   extern __shared__ __align__(16) unsigned char fsm[];
   const int J = a.J, M = a.M, tau = a.tau;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   const bool right = a.censoring == 1;
+  const int jw = warp;  // this warp's state in the window passes (nw == J)
+  // K = 0: the window rings and eta accumulators (shared memory when they
+  // fit, else global scratch and eta itself)
   double* rings = a.rings_in_smem ? (double*)fsm : a.ring;
   double* Wf = rings;                          // [J][M] forward W, by segment start % M
   double* Vb = Wf + (size_t)J * M;             // [J][M] backward V, by segment end % M
-  // eta accumulators: in shared memory with the rings (a global
-  // read-modify-write per duration and step would put the L2 latency on the
-  // backward chain), copied out at the end
   double* Et = a.rings_in_smem ? Vb + (size_t)J * M : a.eta;
   __shared__ double s_r[32], s_F[32], s_S[32], s_G[32], s_q[32];
   __shared__ int s_bad;
@@ -241,6 +261,14 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
   const int gj = warp * per_warp + lane / Gs;  // this lane's state in the grouped sums
   const int gi = lane % Gs;                     // and its i (or k)
   const bool glead = gi == 0 && gj < J;
+  constexpr int KR = K > 0 ? K : 1;
+  double dk[KR], wk[KR], vk[KR], ek[KR];  // K > 0: d(u), W(u), V(u), eta accumulator of u = lane + 1 + 32k
+#pragma unroll
+  for (int k = 0; k < KR; ++k) {
+    const int u = lane + 1 + 32 * k;
+    dk[k] = (K > 0 && jw < J && u <= M) ? dd(jw, u) : 0.0;
+    wk[k] = vk[k] = ek[k] = 0.0;
+  }
 
   if (tid == 0) s_bad = 0;
   for (int j = warp; j < J; j += nw)
@@ -248,9 +276,9 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
       double x = 0;
       for (int v = u; v <= M; ++v) x += dd(j, v);
       a.D[(size_t)j * (M + 1) + u] = x;
-      Et[(size_t)j * M + (u - 1)] = 0.0;
+      if (K == 0) Et[(size_t)j * M + (u - 1)] = 0.0;
     }
-  if (tid < 32) s_S[tid] = 0.0;
+  if (tid < 32) s_S[tid] = s_q[tid] = 0.0;
   __syncthreads();
 
   // ---- forward ----
@@ -264,7 +292,7 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
       const double pdf_nx = (has && t + 1 < tau) ? atc(a.pdf, lane, t + 1) : 0.0;
       double raw = 0.0;
       if (has) raw = t == 0 ? pdf_cur * a.pi[lane] : pdf_cur * (Scur - Fprev + Nmprev);
-      const double n = warp_sum(raw);
+      const double n = group_sum(raw, Gs);
       const double inv = 1.0 / n;
       if (has) {
         const double nm = raw * inv;
@@ -284,22 +312,39 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
     if (s_bad) break;
     const bool last = t == tau - 1;
     const int umax = min(t + 1, M);
-    for (int j = warp; j < J; j += nw) {
-      const double r = s_r[j];
-      double* W = Wf + (size_t)j * M;
+    if (jw < J) {
+      const double r = s_r[jw];
+      // a new segment start takes StateIn (or pi for s = 0)
+      const double sin = t > 0 ? s_S[jw] : a.pi[jw];
       double part = 0.0;
-      for (int u = lane + 1; u <= umax; u += 32) {
-        const int s = t - u + 1;
-        const int slot = s % M;
-        // a new segment start takes StateIn (or pi for s = 0) once
-        const double w = (u == 1) ? r * (t > 0 ? s_S[j] : a.pi[j]) : W[slot] * r;
-        W[slot] = w;
-        part += w * (last ? DD(j, u) : dd(j, u));
+      if constexpr (K > 0) {
+        double carry = 0.0;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          if (32 * k < umax) {
+            // W(u) of step t is W(u-1) of step t-1 times r
+            const double up = __shfl_up_sync(0xffffffffu, wk[k], 1);
+            const double top = __shfl_sync(0xffffffffu, wk[k], 31);
+            const double prev = lane == 0 ? (k == 0 ? sin : carry) : up;
+            carry = top;
+            wk[k] = prev * r;
+            const int u = lane + 1 + 32 * k;
+            if (u <= umax) part = __fma_rn(wk[k], last ? DD(jw, u) : dk[k], part);
+          }
+        }
+      } else {
+        double* W = Wf + (size_t)jw * M;
+        for (int u = lane + 1; u <= umax; u += 32) {
+          const int slot = (t - u + 1) % M;
+          const double w = (u == 1 ? sin : W[slot]) * r;
+          W[slot] = w;
+          part = __fma_rn(w, last ? DD(jw, u) : dd(jw, u), part);
+        }
       }
       const double f = warp_sum(part);
       if (lane == 0) {
-        s_F[j] = f;
-        at(a.F, j, t) = f;
+        s_F[jw] = f;
+        at(a.F, jw, t) = f;
         if (!(f > 0)) s_bad = 1;
       }
     }
@@ -330,10 +375,9 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
   }
 
   // ---- backward ----
-  // warp j (a warp per state): r = pdf/N of step t+1 and the eta weight of
-  // step t, loaded during step t+1; the group leader of state j: F[j][t],
-  // StateIn[j][t+1] likewise, and L[j][t+1] from the previous step
-  const int jw = warp;  // nw == J
+  // warp j: r = pdf/N of step t+1 and the eta weight of step t, loaded
+  // during step t+1; the group leader of state j: F[j][t], StateIn[j][t+1]
+  // likewise, and L[j][t+1] from the previous step
   double r_nx = 0.0, A_nx = 0.0, s_tail = 1.0;
   if (jw < J && tau >= 2) {
     r_nx = at(a.R, jw, tau - 1);
@@ -358,31 +402,58 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
       A_nx = at(a.A, jw, t - 1);
     }
     if (jw < J) {
-      const int j = jw;
       s_tail = s_tail * r;  // the reference's s: r[tau-1] * r[tau-2] * ... * r[t+1]
-      double* V = Vb + (size_t)j * M;
+      const double q = s_q[jw];  // L1(t+1) / F(t+1)
       double part = 0.0;
-      for (int u = lane + 1; u <= umax; u += 32) {
-        const int e = t + u;
-        double h;
-        if (u < span) {
-          const int slot = e % M;
-          const double v = (u == 1) ? r * s_q[j] : V[slot] * r;  // s_q[j] = L1(t+1) / F(t+1)
-          V[slot] = v;
-          h = v * dd(j, u);
-          Et[(size_t)j * M + (u - 1)] += A * h;
-        } else {
-          h = s_tail * DD(j, span);
+      if constexpr (K > 0) {
+        double carry = 0.0;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          if (32 * k < umax) {
+            // V(u) of step t is V(u-1) of step t+1 times r
+            const double up = __shfl_up_sync(0xffffffffu, vk[k], 1);
+            const double top = __shfl_sync(0xffffffffu, vk[k], 31);
+            const double prev = lane == 0 ? (k == 0 ? q : carry) : up;
+            carry = top;
+            vk[k] = prev * r;
+            const int u = lane + 1 + 32 * k;
+            if (u < span && u <= M) {
+              part = __fma_rn(vk[k], dk[k], part);
+              ek[k] = __fma_rn(A, vk[k], ek[k]);
+            } else if (u == span) {
+              part = __fma_rn(s_tail, DD(jw, span), part);
+            }
+          }
         }
-        part += h;
+        if (right && span <= M) {
+#pragma unroll
+          for (int k = 0; k < K; ++k) {
+            const int u = lane + 1 + 32 * k;
+            if (u >= span && u <= M) ek[k] = __fma_rn(A, s_tail, ek[k]);
+          }
+        }
+      } else {
+        double* V = Vb + (size_t)jw * M;
+        double* E = Et + (size_t)jw * M;
+        for (int u = lane + 1; u <= umax; u += 32) {
+          if (u < span) {
+            const int slot = (t + u) % M;
+            const double v = (u == 1 ? q : V[slot]) * r;
+            V[slot] = v;
+            part = __fma_rn(v, dd(jw, u), part);
+            E[u - 1] = __fma_rn(A, v, E[u - 1]);
+          } else {
+            part = __fma_rn(s_tail, DD(jw, span), part);
+          }
+        }
+        if (right && span <= M)
+          for (int u = lane + 1; u <= M; u += 32)
+            if (u >= span) E[u - 1] = __fma_rn(A, s_tail, E[u - 1]);
       }
-      if (right && span <= M)
-        for (int u = lane + 1; u <= M; u += 32)
-          if (u >= span) Et[(size_t)j * M + (u - 1)] += A * (s_tail * dd(j, u));
       const double g = warp_sum(part);
       if (lane == 0) {
-        s_G[j] = g;
-        at(a.G, j, t + 1) = g;
+        s_G[jw] = g;
+        at(a.G, jw, t + 1) = g;
       }
     }
     __syncthreads();
@@ -400,29 +471,42 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
         const double lv = l1 + Lnext - s_G[gj] * st1;
         at(a.L, gj, t) = lv;
         Lnext = lv;
-        s_q[gj] = l1 / f_t;
+        s_q[gj] = sv;
       }
     }
     __syncthreads();
   }
 
-  // eta: the segment that starts at t = 0 (FBImpl.cpp:252-266)
-  for (int j = warp; j < J; j += nw)
-    for (int u = lane + 1; u <= M; u += 32) {
-      if (!(right || u <= tau - 1)) continue;
-      double r = dd(j, u) * a.pi[j];
-      if (u <= tau - 1) {
-        for (int v = 1; v <= u; ++v) r *= atc(a.pdf, j, u - v) / a.N[u - v];
-        r *= at(a.L1, j, u - 1) / at(a.F, j, u - 1);
+  // eta = d(u) * (accumulated A * V and A * s) + the segment that starts at
+  // t = 0 (FBImpl.cpp:252-266)
+  if (jw < J) {
+    const int j = jw;
+    for (int k = 0, u = lane + 1; u <= M; ++k, u += 32) {
+      double w;
+      if constexpr (K > 0) {
+        double e = 0.0, dv = 0.0;
+#pragma unroll
+        for (int m = 0; m < K; ++m)
+          if (m == k) {
+            e = ek[m];
+            dv = dk[m];
+          }
+        w = e * dv;
       } else {
-        for (int v = 1; v <= tau; ++v) r *= atc(a.pdf, j, tau - v) / a.N[tau - v];
+        w = Et[(size_t)j * M + (u - 1)] * dd(j, u);
       }
-      Et[(size_t)j * M + (u - 1)] += r;
+      if (right || u <= tau - 1) {
+        double r = dd(j, u) * a.pi[j];
+        if (u <= tau - 1) {
+          for (int v = 1; v <= u; ++v) r *= atc(a.pdf, j, u - v) / a.N[u - v];
+          r *= at(a.L1, j, u - 1) / at(a.F, j, u - 1);
+        } else {
+          for (int v = 1; v <= tau; ++v) r *= atc(a.pdf, j, tau - v) / a.N[tau - v];
+        }
+        w += r;
+      }
+      a.eta[(size_t)j * M + (u - 1)] = w;
     }
-  if (a.rings_in_smem) {
-    __syncthreads();
-    for (int j = warp; j < J; j += nw)
-      for (int u = lane + 1; u <= M; u += 32) a.eta[(size_t)j * M + (u - 1)] = Et[(size_t)j * M + (u - 1)];
   }
   if (tid == 0) *a.status = 0;
 }

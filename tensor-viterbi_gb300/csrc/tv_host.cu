@@ -928,11 +928,13 @@ int fb_run(int censoring, int64_t tau, int J, int M, const double* d, const doub
   int dev = 0, smem_optin = 0;
   TV_CUDA(cudaGetDevice(&dev));
   TV_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  // J <= 32: the short-chain kernel (a forward and a backward ring, the
-  // ratios and eta weights kept for the backward pass); otherwise the
-  // general one
+  // J <= 32: the short-chain kernel (a warp per state, the ratios and eta
+  // weights kept for the backward pass), with the window in registers up to
+  // 32 * FB_REG_BLOCKS durations and in rings (forward, backward, eta
+  // accumulators) beyond; otherwise the general one
   const bool small = J <= 32;
-  const size_t nrings = small ? 3 : 2;  // small: forward and backward rings + eta accumulators
+  const bool regs = small && M <= 32 * tv::FB_REG_BLOCKS;
+  const size_t nrings = regs ? 0 : small ? 3 : 2;
   const size_t ring_bytes = nrings * JM * sizeof(double);
   const bool in_smem = ring_bytes + 2048 <= (size_t)smem_optin;
   if (!in_smem && b.get(&dring, nrings * JM)) return fail(TV_ENOMEM, "tv_fb: device allocation failed");
@@ -955,12 +957,14 @@ int fb_run(int censoring, int64_t tau, int J, int M, const double* d, const doub
   A.R = dR; A.A = dA;
   const int threads = 32 * std::min(32, J);
   const size_t dyn = in_smem ? ring_bytes : 0;
-  const void* kern = small ? (const void*)tv::fb_small_kernel : (const void*)tv::fb_kernel;
+  const void* kern = regs ? (const void*)tv::fb_small_kernel<tv::FB_REG_BLOCKS>
+                     : small ? (const void*)tv::fb_small_kernel<0> : (const void*)tv::fb_kernel;
   if (dyn) {
     int rc = raise_smem_limit(kern);
     if (rc != TV_OK) return rc;
   }
-  if (small) tv::fb_small_kernel<<<1, threads, dyn>>>(A);
+  if (regs) tv::fb_small_kernel<tv::FB_REG_BLOCKS><<<1, threads, dyn>>>(A);
+  else if (small) tv::fb_small_kernel<0><<<1, threads, dyn>>>(A);
   else tv::fb_kernel<<<1, threads, dyn>>>(A);
   TV_CUDA(cudaGetLastError());
   int st = 0;

@@ -38,7 +38,13 @@ def test_gpu_forward_backward_matches_the_reference(tvlib, name):
         _close(r[k], z[k], k)
 
 
-@pytest.mark.parametrize("J,M,tau,cens", [(20, 200, 3000, 1), (7, 333, 1200, 0), (40, 64, 2000, 1), (3, 5, 4000, 1)])
+# J <= 32 and M <= 128: the window in registers (M = 5, 100, 128: one, four
+# partial and four full blocks of 32 durations, J = 32 a full CTA); M > 128:
+# the shared-memory rings (M = 129, 200, 333) or, past shared memory, global
+# ones (J = 32, M = 300); J > 32: the general kernel.
+@pytest.mark.parametrize("J,M,tau,cens", [(20, 200, 3000, 1), (7, 333, 1200, 0), (40, 64, 2000, 1), (3, 5, 4000, 1),
+                                          (12, 128, 1500, 1), (32, 100, 700, 0), (32, 129, 800, 1),
+                                          (32, 300, 900, 1)])
 def test_gpu_forward_backward_matches_the_oracle_on_random_models(tvlib, J, M, tau, cens):
     rng = np.random.default_rng(J * 1000 + M)
     p = rng.dirichlet(np.ones(J), size=J)
