@@ -204,8 +204,40 @@ __device__ __forceinline__ double group_sum(double v, int g) {
   return v;
 }
 
-// Durations a lane of fb_small_kernel<K> holds in registers: u = lane + 1 + 32k
-// for k < K, so K = ceil(M / 32) blocks cover the window.
+// Sum over the aligned group of g lanes (g a power of two <= 32) of finite
+// doubles, formed in 64-bit integers: each lane's significand is aligned to
+// the group's largest exponent (with five bits of headroom for 32 terms) and
+// truncated there, the integers are summed exactly by shuffles, and the sum
+// is converted to double once, so the FP64 unit runs one conversion instead
+// of log2(g) dependent adds.  Error: below 2^-52 of the largest term's
+// magnitude (the same order as a tree of double adds).  A group holding an
+// infinity or NaN is summed with double adds.
+__device__ __forceinline__ double fixed_group_sum(double v, int g) {
+  const unsigned full = 0xffffffffu;
+  if (__any_sync(full, ((__double_as_longlong(v) >> 52) & 0x7ff) == 0x7ff)) return group_sum(v, g);
+  const long long b = __double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7ff);
+  const long long m = (b & 0xfffffffffffffLL) | (e ? (1LL << 52) : 0LL);
+  const int ee = e ? e : 1;  // subnormals share the smallest normal exponent
+  int emax = ee;
+  for (int o = g >> 1; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(full, emax, o));
+  const int sh = emax - ee;
+  long long f = sh >= 58 ? 0LL : (m << 5) >> sh;  // units of 2^(emax - 1080)
+  if (b < 0) f = -f;
+  for (int o = g >> 1; o > 0; o >>= 1) f += __shfl_xor_sync(full, f, o);
+  // f * 2^(emax - 1080): exact exponent arithmetic when the result is normal
+  const double c = __ll2double_rn(f);
+  const long long cb = __double_as_longlong(c);
+  const int ce = (int)((cb >> 52) & 0x7ff) + emax - 1080;
+  if (f == 0) return 0.0;
+  if (ce >= 1 && ce <= 2046) return __longlong_as_double((cb & ~(0x7ffLL << 52)) | ((long long)ce << 52));
+  return ldexp(c, emax - 1080);
+}
+
+// Durations a lane of fb_small_kernel<K, MAXT> holds in registers:
+// u = lane + 1 + 32k for k < K, so K blocks of 32 cover a window of up to
+// 32K durations.  MAXT is the launch bound (32 J threads): 512 leaves the
+// register window room without spilling.
 constexpr int FB_REG_BLOCKS = 4;
 
 // fb_small_kernel: the same E step for J <= 32 states, one warp per state.
@@ -220,7 +252,9 @@ constexpr int FB_REG_BLOCKS = 4;
 //             entries live in registers (lane + 32k holds u = lane + 1 + 32k)
 //             and move up one duration per step by warp shuffles; with K = 0
 //             in a shared-memory ring indexed by the segment start.  F is the
-//             sum of W(u) * dur(u), fused multiply-adds and a warp reduction;
+//             sum of W(u) * dur(u): fused multiply-adds, then a warp
+//             reduction in 64-bit integers (fixed_group_sum: ten warps of
+//             double-add trees would occupy the SM's FP64 unit);
 //             groups of lanes (a power of two >= J per state) form
 //             StateIn[j][t+1] and the eta weight A[j][t] = sum_{i != j} p[i][j] F[i][t].
 //   backward: warp j keeps V(u) = Q(t+1..t+u) * L1(t+u) / F(t+u) for the
@@ -234,8 +268,8 @@ constexpr int FB_REG_BLOCKS = 4;
 // Products, the sums over u, i, k and j, fused multiply-adds and the
 // divisions associate differently from the reference (which sums in order
 // and divides each term), which moves results by rounding only.
-template <int K>
-__global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
+template <int K, int MAXT>
+__global__ void __launch_bounds__(MAXT) fb_small_kernel(FbArgs a) {
   extern __shared__ __align__(16) unsigned char fsm[];
   const int J = a.J, M = a.M, tau = a.tau;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
@@ -341,7 +375,7 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
           part = __fma_rn(w, last ? DD(jw, u) : dd(jw, u), part);
         }
       }
-      const double f = warp_sum(part);
+      const double f = fixed_group_sum(part, 32);
       if (lane == 0) {
         s_F[jw] = f;
         at(a.F, jw, t) = f;
@@ -450,7 +484,7 @@ __global__ void __launch_bounds__(1024) fb_small_kernel(FbArgs a) {
           for (int u = lane + 1; u <= M; u += 32)
             if (u >= span) E[u - 1] = __fma_rn(A, s_tail, E[u - 1]);
       }
-      const double g = warp_sum(part);
+      const double g = fixed_group_sum(part, 32);
       if (lane == 0) {
         s_G[jw] = g;
         at(a.G, jw, t + 1) = g;

@@ -957,15 +957,18 @@ int fb_run(int censoring, int64_t tau, int J, int M, const double* d, const doub
   A.R = dR; A.A = dA;
   const int threads = 32 * std::min(32, J);
   const size_t dyn = in_smem ? ring_bytes : 0;
-  const void* kern = regs ? (const void*)tv::fb_small_kernel<tv::FB_REG_BLOCKS>
-                     : small ? (const void*)tv::fb_small_kernel<0> : (const void*)tv::fb_kernel;
+  constexpr int KR = tv::FB_REG_BLOCKS;
+  const void* kern = !small ? (const void*)tv::fb_kernel
+                     : !regs ? (const void*)tv::fb_small_kernel<0, 1024>
+                     : J <= 16 ? (const void*)tv::fb_small_kernel<KR, 512> : (const void*)tv::fb_small_kernel<KR, 1024>;
   if (dyn) {
     int rc = raise_smem_limit(kern);
     if (rc != TV_OK) return rc;
   }
-  if (regs) tv::fb_small_kernel<tv::FB_REG_BLOCKS><<<1, threads, dyn>>>(A);
-  else if (small) tv::fb_small_kernel<0><<<1, threads, dyn>>>(A);
-  else tv::fb_kernel<<<1, threads, dyn>>>(A);
+  if (!small) tv::fb_kernel<<<1, threads, dyn>>>(A);
+  else if (!regs) tv::fb_small_kernel<0, 1024><<<1, threads, dyn>>>(A);
+  else if (J <= 16) tv::fb_small_kernel<KR, 512><<<1, threads, dyn>>>(A);
+  else tv::fb_small_kernel<KR, 1024><<<1, threads, dyn>>>(A);
   TV_CUDA(cudaGetLastError());
   int st = 0;
   TV_CUDA(cudaMemcpy(&st, dst, sizeof(int), cudaMemcpyDeviceToHost));

@@ -58,6 +58,23 @@ def test_gpu_forward_backward_matches_the_oracle_on_random_models(tvlib, J, M, t
         _close(got[k], want[k], k)
 
 
+@pytest.mark.parametrize("J,M", [(6, 40), (24, 150)])
+def test_gpu_forward_backward_over_a_wide_likelihood_range(tvlib, J, M):
+    """Likelihoods from 1e-250 to 1: window sums whose terms span hundreds of
+    binary orders (the integer-aligned reductions drop the smallest)."""
+    rng = np.random.default_rng(J + 7 * M)
+    tau = 900
+    p = rng.dirichlet(np.ones(J), size=J)
+    d = rng.dirichlet(np.ones(M), size=J)
+    pi = rng.dirichlet(np.ones(J))
+    pdf = 10.0 ** rng.uniform(-250.0, 0.0, size=(J, tau))
+    want = orc.forward_backward(1, d, p, pi, pdf)
+    got = tvlib.forward_backward(1, d, p, pi, pdf)
+    assert got["err"] == want["err"] == 0
+    for k in orc.FB_KEYS:
+        _close(got[k], want[k], k)
+
+
 def test_gpu_forward_backward_reports_a_zero_normaliser(tvlib):
     z = np.load(FB / "fb_J3_M20_T300_c1.npz")
     pdf = z["pdf"].copy()
