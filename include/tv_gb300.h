@@ -161,6 +161,18 @@ int tv_grid_plan_info(int N, int D, int G, int smem_optin, int force_l2, int64_t
  * round-trip CTAs}.  Synchronous; allocates and frees its own buffers. */
 int tv_step_floor(int n_states, int max_dur, int64_t steps, double* out);
 
+/* One SM's FP64 unit (diagnostics for benchmark reporting; no reference
+ * counterpart): the bound of tv_fb, whose sequence runs on one SM.
+ * out[0..3] = {FP64 warp instructions per clock with 8 warps of 8
+ * independent fused multiply-add chains, that SM's FP64 FLOP/s (an FMA is two,
+ * CUDA events), the SM clock over the run in MHz, clocks per dependent FP64
+ * instruction of one warp}.  Synchronous. */
+int tv_fp64_peak(double* out);
+
+/* Device time in milliseconds of the calling thread's last tv_fb kernel
+ * (CUDA events around its launch; copies excluded); 0 before any call. */
+double tv_fb_last_kernel_ms(void);
+
 /* Kernel timing for benchmark reporting (no reference counterpart).  When
  * enabled, CUDA events on the decode's own stream bracket its main kernel;
  * tv_model_kernel_ms waits for that kernel and returns its time in ms for

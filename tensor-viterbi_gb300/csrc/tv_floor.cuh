@@ -20,10 +20,35 @@
 // stores and bounded polling loads: the latency a head-worker message pays,
 // hidden in the decoder by the workers' L-step lead.
 //
+// fp64_issue_kernel measures one SM's FP64 unit, the bound of the
+// forward-backward kernel (one sequence runs on one SM): with several warps
+// of threads each running eight independent fused multiply-add chains, the
+// SM's FP64 issue rate; with one warp and one chain, the dependent latency of
+// one FP64 instruction.
+//
 // This file is included by tv_host.cu after tv_grid.cuh.
 #pragma once
 
 namespace tv {
+
+__global__ void fp64_issue_kernel(int independent, long long iters, const double* __restrict__ in, double* sink,
+                                  unsigned long long* clk) {
+  const double y = in[8], z = in[9];
+  double a0 = in[0], a1 = in[1], a2 = in[2], a3 = in[3], a4 = in[4], a5 = in[5], a6 = in[6], a7 = in[7];
+  __syncthreads();
+  const long long t0 = clock64();
+  if (independent) {
+    for (long long i = 0; i < iters; ++i) {
+      a0 = __fma_rn(a0, y, z); a1 = __fma_rn(a1, y, z); a2 = __fma_rn(a2, y, z); a3 = __fma_rn(a3, y, z);
+      a4 = __fma_rn(a4, y, z); a5 = __fma_rn(a5, y, z); a6 = __fma_rn(a6, y, z); a7 = __fma_rn(a7, y, z);
+    }
+  } else {
+    for (long long i = 0; i < iters; ++i) a0 = __fma_rn(a0, y, z);
+  }
+  const long long t1 = clock64();
+  sink[threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if ((threadIdx.x & 31) == 0) atomicMax(clk, (unsigned long long)(t1 - t0));
+}
 
 __global__ void floor_chain_kernel(int N, int Np, int split, long long steps, const double* __restrict__ trans,
                                    double scale, int sh, long long* out) {

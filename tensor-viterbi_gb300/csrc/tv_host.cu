@@ -885,11 +885,14 @@ int read_status(tv_model_s* m, int n_seq, cudaStream_t st) {
 // Device buffers freed together when the arena goes out of scope.
 struct DevArena {
   std::vector<void*> p;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
   DevArena() = default;
   DevArena(const DevArena&) = delete;
   DevArena& operator=(const DevArena&) = delete;
   ~DevArena() {
     for (void* q : p) cudaFree(q);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
   }
   template <class T>
   int get(T** out, size_t n) {
@@ -903,6 +906,10 @@ struct DevArena {
     return TV_OK;
   }
 };
+
+// Device time of the calling thread's last forward-backward kernel (CUDA
+// events around the launch).
+thread_local double g_fb_kernel_ms = 0.0;
 
 // The forward-backward E step (tv_fb): device copies of the inputs and
 // outputs, one launch, copies back.
@@ -965,11 +972,19 @@ int fb_run(int censoring, int64_t tau, int J, int M, const double* d, const doub
     int rc = raise_smem_limit(kern);
     if (rc != TV_OK) return rc;
   }
+  TV_CUDA(cudaEventCreate(&b.e0));
+  TV_CUDA(cudaEventCreate(&b.e1));
+  TV_CUDA(cudaEventRecord(b.e0));
   if (!small) tv::fb_kernel<<<1, threads, dyn>>>(A);
   else if (!regs) tv::fb_small_kernel<0, 1024><<<1, threads, dyn>>>(A);
   else if (J <= 16) tv::fb_small_kernel<KR, 512><<<1, threads, dyn>>>(A);
   else tv::fb_small_kernel<KR, 1024><<<1, threads, dyn>>>(A);
   TV_CUDA(cudaGetLastError());
+  TV_CUDA(cudaEventRecord(b.e1));
+  TV_CUDA(cudaEventSynchronize(b.e1));
+  float kms = 0.0f;
+  TV_CUDA(cudaEventElapsedTime(&kms, b.e0, b.e1));
+  g_fb_kernel_ms = (double)kms;
   int st = 0;
   TV_CUDA(cudaMemcpy(&st, dst, sizeof(int), cudaMemcpyDeviceToHost));
   TV_CUDA(cudaMemcpy(F, dF, sizeof(double) * JT, cudaMemcpyDeviceToHost));
@@ -1452,6 +1467,53 @@ int tv_fb(int censoring, int64_t tau, int J, int M, const double* d, const doubl
           const double* pdf, double* F, double* L, double* G, double* L1, double* Nn, double* Norm,
           double* eta) {
   return fb_run(censoring, tau, J, M, d, p, pi, pdf, F, L, G, L1, Nn, Norm, eta);
+}
+
+double tv_fb_last_kernel_ms(void) { return g_fb_kernel_ms; }
+
+int tv_fp64_peak(double* out) {
+  if (!out) return fail(TV_EINVAL, "tv_fp64_peak: out is null");
+  int devs = 0;
+  if (cudaGetDeviceCount(&devs) != cudaSuccess || devs == 0) return fail(TV_ENODEV, "no CUDA device");
+  DevArena b;
+  double *din, *sink;
+  unsigned long long* clk;
+  if (b.get(&din, 16) || b.get(&sink, 1024) || b.get(&clk, 1)) return fail(TV_ENOMEM, "tv_fp64_peak: allocation");
+  double h[16];
+  for (int i = 0; i < 8; ++i) h[i] = 1.0 + 0.125 * i;
+  h[8] = 0.999999;  // the chains converge to z / (1 - y): finite
+  h[9] = 1e-3;
+  for (int i = 10; i < 16; ++i) h[i] = 0.0;
+  TV_CUDA(cudaMemcpy(din, h, sizeof h, cudaMemcpyHostToDevice));
+  TV_CUDA(cudaEventCreate(&b.e0));
+  TV_CUDA(cudaEventCreate(&b.e1));
+  const int warps = 8;
+  const long long iters = 1 << 15;
+  unsigned long long hc = 0;
+  // issue rate: 8 warps x 8 independent chains (warm-up launch first)
+  for (int rep = 0; rep < 2; ++rep) {
+    TV_CUDA(cudaMemset(clk, 0, sizeof(unsigned long long)));
+    TV_CUDA(cudaEventRecord(b.e0));
+    tv::fp64_issue_kernel<<<1, 32 * warps>>>(1, rep ? iters : 1024, din, sink, clk);
+    TV_CUDA(cudaGetLastError());
+    TV_CUDA(cudaEventRecord(b.e1));
+    TV_CUDA(cudaEventSynchronize(b.e1));
+  }
+  TV_CUDA(cudaMemcpy(&hc, clk, sizeof hc, cudaMemcpyDeviceToHost));
+  float ms = 0.0f;
+  TV_CUDA(cudaEventElapsedTime(&ms, b.e0, b.e1));
+  const double warp_insts = (double)warps * 8.0 * (double)iters;
+  out[0] = warp_insts / (double)std::max(hc, 1ULL);                   // FP64 warp instructions per clock, one SM
+  out[1] = warp_insts * 32.0 * 2.0 / ((double)ms * 1e-3);              // FLOP/s of one SM (an FMA is two)
+  out[2] = (double)hc / ((double)ms * 1e-3) / 1e6;                     // SM clock over the run, MHz
+  // dependent latency: one warp, one chain
+  TV_CUDA(cudaMemset(clk, 0, sizeof(unsigned long long)));
+  tv::fp64_issue_kernel<<<1, 32>>>(0, iters, din, sink, clk);
+  TV_CUDA(cudaGetLastError());
+  TV_CUDA(cudaDeviceSynchronize());
+  TV_CUDA(cudaMemcpy(&hc, clk, sizeof hc, cudaMemcpyDeviceToHost));
+  out[3] = (double)hc / (double)iters;                                 // clocks per dependent FP64 instruction
+  return TV_OK;
 }
 
 int tv_step_floor(int n_states, int max_dur, int64_t steps, double* out) {

@@ -55,6 +55,8 @@ EXPORTS = {
     "tv_model_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "tv_model_kernel_ms": (C.c_double, [C.c_void_p]),
     "tv_step_floor": (C.c_int, [C.c_int, C.c_int, C.c_int64, _dp]),
+    "tv_fp64_peak": (C.c_int, [_dp]),
+    "tv_fb_last_kernel_ms": (C.c_double, []),
     "tv_fb": (C.c_int, [C.c_int, C.c_int64, C.c_int, C.c_int] + [_dp] * 11),
     "tv_decode_device_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p]),

@@ -382,6 +382,21 @@ def step_floor(n_states: int, max_dur: int, steps: int = 20000) -> dict:
             "roundtrip_sms": [int(out[5]), int(out[6])]}
 
 
+def fp64_peak() -> dict:
+    """One SM's FP64 unit (diagnostics): issue rate with eight warps of
+    independent fused multiply-add chains, that SM's FLOP/s, the SM clock over
+    the run, and the dependent latency of one FP64 instruction."""
+    out = np.zeros(4, dtype=np.float64)
+    _lib.check(_lib.lib().tv_fp64_peak(_lib.dptr(out)))
+    return {"warp_insts_per_clock": float(out[0]), "flops": float(out[1]), "sm_mhz": float(out[2]),
+            "dependent_clocks": float(out[3])}
+
+
+def fb_last_kernel_ms() -> float:
+    """Device time of this thread's last forward_backward kernel (ms)."""
+    return float(_lib.lib().tv_fb_last_kernel_ms())
+
+
 def forward_backward(censoring, d, p, pi, pdf) -> dict:
     """The forward-backward E step of HSMM training on the GPU (tv_fb), with
     hsmmlearn's _fb_impl arguments and layouts (hsmmlearn/hsmmlearn/base.pyx):

@@ -75,6 +75,20 @@ def test_gpu_forward_backward_over_a_wide_likelihood_range(tvlib, J, M):
         _close(got[k], want[k], k)
 
 
+def test_fp64_probe_and_kernel_timing(tvlib):
+    """The FP64 probe that sets the forward-backward roofline returns a
+    plausible unit (a warp instruction per few to a hundred clocks, a
+    dependent latency of a few to a thousand clocks), and the kernel's own
+    event time is recorded."""
+    pk = tvlib.fp64_peak()
+    assert 0.005 < pk["warp_insts_per_clock"] <= 4.0
+    assert 4.0 <= pk["dependent_clocks"] <= 1000.0
+    assert pk["flops"] > 1e8 and 500.0 < pk["sm_mhz"] < 5000.0
+    z = np.load(FB / "fb_J8_M60_T800_c1.npz")
+    tvlib.forward_backward(1, z["d"], z["p"], z["pi"], z["pdf"])
+    assert tvlib.fb_last_kernel_ms() > 0.0
+
+
 def test_gpu_forward_backward_reports_a_zero_normaliser(tvlib):
     z = np.load(FB / "fb_J3_M20_T300_c1.npz")
     pdf = z["pdf"].copy()
