@@ -890,6 +890,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true",
                     help="skip the host-buffer (drop-in call) measurement: long stress workloads")
     ap.add_argument("--T", type=int, default=0, help="override the sequence length (profiling runs)")
+    ap.add_argument("--n-seq", type=int, default=0, help="batched workload: override the number of sequences "
+                                                         "(profiling runs)")
     ap.add_argument("--loads", default="", help="served workload: comma-separated fractions of the capacity")
     ap.add_argument("--requests", type=int, default=0, help="served workload: number of requests per rate")
     ap.add_argument("--capacity-requests", type=int, default=1000,
@@ -898,6 +900,8 @@ def main():
     w = dict(WORKLOADS[args.workload])
     if args.T:
         w["T"] = args.T
+    if args.n_seq:
+        w["n_seq"] = args.n_seq
     if args.requests:
         w["n_req"] = args.requests
     if w.get("kind") == "served":
