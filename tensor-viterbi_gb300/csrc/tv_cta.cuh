@@ -178,10 +178,16 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
     }
     __syncthreads();
 
+    // Ring positions kept incrementally (a 64-bit remainder by a runtime
+    // divisor is a long dependent integer sequence): r0 = (t-1) % D, the slot
+    // of s = t-1 in ctil/itil/acc, and rt = t % (D+1), the row of step t in
+    // dstar.  The observation of step t+1 is loaded a step ahead.
+    int r0 = 0, rt = 1 % (D + 1);
+    int ot_nx = T > 1 ? obs[1] : 0;
     for (long long t = 1; t < T; ++t) {
       const int tau = (int)(t < D ? t : D);
-      const int ot = obs[t];
-      const int r0 = (int)((t - 1) % D);  // ring slot of s = t-1 (d = 0)
+      const int ot = ot_nx;
+      if (t + 1 < T) ot_nx = obs[t + 1];
 
       // Phase 0 (t <= D): the reference rebuilds the window sums newest-first,
       // E_t[d] = E_t[d-1] + em_{t-d} (src/hsmm.cu:311-322).  One chain per
@@ -282,12 +288,13 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
         } else {
           int r1 = r0 - bd;
           if (r1 < 0) r1 += D;
-          const long long s1 = t - 1 - bd;
+          int rs = rt - 1 - bd;  // (t-1-bd) % (D+1), 0 <= bd < D
+          if (rs < 0) rs += D + 1;
           const double e = acc[(size_t)j * D + r1];
-          const double dp = dstar[(size_t)(s1 % (D + 1)) * N + bi];
+          const double dp = dstar[(size_t)rs * N + bi];
           vbest = (e + dp) + (m.trans[(size_t)j * N + bi] + m.durT[(size_t)j * D + bd]);
         }
-        double* slot = dstar + (size_t)(t % (D + 1)) * N + j;
+        double* slot = dstar + (size_t)rt * N + j;
         // For t < D the induction result replaces the initialisation value
         // only when strictly larger (src/hsmm.cu:353-358).
         double fin;
@@ -304,6 +311,8 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
         psi[(size_t)t * N + j] = pw;
       }
       __syncthreads();
+      r0 = r0 + 1 == D ? 0 : r0 + 1;
+      rt = rt + 1 == D + 1 ? 0 : rt + 1;
     }
 
     // Tail adjustment at t = T-1 (src/hsmm.cu:101-137): survival in place of
