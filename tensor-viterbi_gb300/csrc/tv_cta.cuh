@@ -56,15 +56,20 @@ struct CtaLayout {
   unsigned long long o_qd, o_ctil, o_acc, o_dstar, o_itil, o_qtr, o_dq, o_ptil, o_tail;
   unsigned long long bytes;
   int in_smem;
+  int qd_global;  // qd read from the model's table in global memory (through L1), not copied per CTA
 };
 
 __host__ __device__ inline unsigned long long tv_align(unsigned long long x) { return (x + 15ull) & ~15ull; }
 
-__host__ inline CtaLayout make_cta_layout(int N, int D) {
+// qd_global: leave the quantised duration table (8 N D bytes, the same for
+// every CTA) out of the work area, so that more CTAs share an SM's shared
+// memory; the scan then reads it from global memory, cached in L1.
+__host__ inline CtaLayout make_cta_layout(int N, int D, bool qd_global = false) {
   CtaLayout L{};
   unsigned long long o = 0;
   const unsigned long long nd = (unsigned long long)N * D;
-  L.o_qd = o;    o = tv_align(o + nd * 8);
+  L.qd_global = qd_global ? 1 : 0;
+  L.o_qd = o;    if (!qd_global) o = tv_align(o + nd * 8);
   L.o_ctil = o;  o = tv_align(o + nd * 8);
   L.o_acc = o;   o = tv_align(o + nd * 8);
   L.o_dstar = o; o = tv_align(o + (unsigned long long)(D + 1) * N * 8);
@@ -114,7 +119,8 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   unsigned char* base = L.in_smem ? smem : scratch + (size_t)blockIdx.x * L.bytes;
-  long long* qd = (long long*)(base + L.o_qd);
+  long long* qd_w = (long long*)(base + L.o_qd);
+  const long long* qd = L.qd_global ? m.qdurT : qd_w;
   long long* ctil = (long long*)(base + L.o_ctil);
   double* acc = (double*)(base + L.o_acc);
   double* dstar = (double*)(base + L.o_dstar);
@@ -132,7 +138,8 @@ __global__ void __launch_bounds__(NTHREADS) cta_decode_kernel(ModelView m, Batch
   while (G < 32 && G * 4 < N) G <<= 1;
 
   // Model tables shared by every sequence of the batch.
-  for (size_t k = threadIdx.x; k < (size_t)N * D; k += NTHREADS) qd[k] = m.qdurT[k];
+  if (!L.qd_global)
+    for (size_t k = threadIdx.x; k < (size_t)N * D; k += NTHREADS) qd_w[k] = m.qdurT[k];
   for (size_t k = threadIdx.x; k < (size_t)N * N; k += NTHREADS) qtr[k] = m.qtr[k];
 
   for (;;) {

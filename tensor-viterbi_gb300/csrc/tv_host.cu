@@ -342,13 +342,18 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
     order_dev = m->order.p;
   }
 
-  tv::CtaLayout L = tv::make_cta_layout(N, D);
   int dev = 0;
   TV_CUDA(cudaGetDevice(&dev));
   int smem_optin = 0;
   TV_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  size_t dyn = 0;
   const size_t static_smem = 64;
+  // Work area in shared memory when it fits; then, per CTA shape, the
+  // duration table stays in global memory when that lets more CTAs share an
+  // SM (the window scan is bound by the SM's FP64 unit and the phases'
+  // barriers, which more resident CTAs overlap).
+  const tv::CtaLayout L_full = tv::make_cta_layout(N, D), L_lean = tv::make_cta_layout(N, D, true);
+  tv::CtaLayout L = L_full;
+  size_t dyn = 0;
   if (L.bytes + static_smem <= (size_t)smem_optin) {
     L.in_smem = 1;
     dyn = L.bytes;
@@ -356,9 +361,15 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
   // grid of a shape: as many CTAs as the SMs hold, at most one per sequence
   auto prepare = [&](int threads, int n, int& grid) -> int {
     const CtaKernelFn kern = cta_kernel_for(threads);
-    if (dyn) {
+    if (L_full.bytes + static_smem <= (size_t)smem_optin) {
       const int rc2 = raise_smem_limit((const void*)kern);
       if (rc2 != TV_OK) return rc2;
+      int pf = 1, pl = 1;
+      TV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pf, kern, threads, L_full.bytes));
+      TV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pl, kern, threads, L_lean.bytes));
+      L = pl > pf ? L_lean : L_full;
+      L.in_smem = 1;
+      dyn = L.bytes;
     }
     int per_sm = 1;
     TV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, dyn));
