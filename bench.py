@@ -832,7 +832,8 @@ def run_batch(args, w, wname):
             "config": {"workload": wname, "n_seq": w["n_seq"], "n_states": N, "max_dur": D, "symbols": w["M"],
                        "lengths": f"log-uniform [{w['lo']:g},{w['hi']:g}]", "total_steps": int(lens.sum()),
                        "l2": "flushed between steps (256 MiB write)", "parallelism": f"sequence shards x{ws}",
-                       "form": "batched, one persistent launch", "cta_threads": model.batch_threads()},
+                       "form": "batched, one persistent launch", "cta_threads": model.batch_threads(),
+                       "cta_grid": model.batch_grid()},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "kernel": "cta_decode_kernel", "kernel_ms": kmean,
                          "algo_bytes_per_launch": ALGO_BYTES_PER_CELL * cells, "peak_source": peak_kind},

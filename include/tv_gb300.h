@@ -122,12 +122,18 @@ int tv_model_last_path(tv_model m);
 /* Threads per CTA of the most recent batched decode on this model, 0 before
  * any (no reference counterpart).  The batched decodes (tv_decode_batch,
  * tv_decode_batch_device) take the CTA shape from an autotuner: the first
- * batch of a (N, D) shape with at least two waves of CTAs times every
- * candidate shape (128, 256, 384, 512 threads) on its own shortest
- * sequences, waiting for those runs, and the fastest is kept for the
- * process.  Setting the environment variable TV_AUTOTUNE=0 keeps the
- * default shape (256).  Results never depend on the shape. */
+ * batch of a (N, D) shape with at least two waves of CTAs runs every
+ * candidate shape (128, 256, 384, 512 threads) for one wave of its own grid
+ * on sequences of 2 D to 8 D steps cut from the batch's observations,
+ * waiting for those runs, and the shape with the most steps per second is
+ * kept for the process.  The trial runs write the batch's output buffers,
+ * which the real decode then overwrites.  Setting the environment variable
+ * TV_AUTOTUNE=0 keeps the default shape (256).  Results never depend on the
+ * shape. */
 int tv_model_batch_threads(tv_model m);
+/* The number of CTAs of the last batched launch (the SM count times the CTAs
+ * that share an SM, at most one per sequence); 0 before any. */
+int tv_model_batch_grid(tv_model m);
 
 /* Failure injection for tests (no reference counterpart; the reference's
  * answer to any device failure is exit(EXIT_FAILURE), src/hsmm.cu:22-30).

@@ -203,9 +203,11 @@ struct tv_model_s {
   DevBuf<int> status;
   DevBuf<int> counter;
   DevBuf<int64_t> off;
-  DevBuf<int> order, tune_order;
+  DevBuf<int> order;
+  DevBuf<int64_t> tune_off;
   DevBuf<unsigned char> scratch;
   int batch_threads = 0;  // CTA shape of the last batched launch
+  int batch_grid = 0;     // and its number of CTAs
   DevBuf<int32_t> obs_tmp, path_tmp;
   DevBuf<double> ll_tmp;
   int64_t last_launches = 0;
@@ -367,7 +369,9 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
       int pf = 1, pl = 1;
       TV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pf, kern, threads, L_full.bytes));
       TV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pl, kern, threads, L_lean.bytes));
-      L = pl > pf ? L_lean : L_full;
+      // only when the batch has more sequences than the full layout's CTAs
+      // can hold (a lone CTA is faster with the table in shared memory)
+      L = (pl > pf && n > m->sm_count * pf) ? L_lean : L_full;
       L.in_smem = 1;
       dyn = L.bytes;
     }
@@ -393,8 +397,11 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
 
   // The CTA shape: the tuned one for this (N, D, placement), else 256.  A
   // batch of at least two waves of CTAs with no tuned shape yet measures
-  // every shape on its own shortest sequences (one wave) and keeps the
-  // fastest; TV_AUTOTUNE=0 turns this off.
+  // every shape and keeps the one with the highest rate; TV_AUTOTUNE=0 turns
+  // this off.  Each shape runs one wave of its own grid (the CTAs that share
+  // an SM differ between shapes) on sequences of 8 D steps cut from the
+  // batch's observations (mostly the steady state of the recurrence, not the
+  // initialisation), and is scored by steps per second.
   int threads = kThreads;
   const auto key = std::make_tuple(N, D, L.in_smem);
   bool tuned = false;
@@ -408,17 +415,9 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
   }
   const char* env = std::getenv("TV_AUTOTUNE");
   const bool tune_on = !(env && env[0] == '0');
-  if (!tuned && tune_on && tune && n_seq >= 2 * m->sm_count) {
-    const int n_s = std::min(n_seq, m->sm_count * 2);
-    // the n_s shortest sequences, longest first, as the sample's order
-    std::vector<int> ord((size_t)n_seq);
-    for (int k = 0; k < n_seq; ++k) ord[k] = k;
-    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
-      return off_host[a + 1] - off_host[a] > off_host[b + 1] - off_host[b];
-    });
-    std::vector<int> sample(ord.end() - n_s, ord.end());
-    if ((rc = m->tune_order.ensure((size_t)n_s)) != TV_OK) return rc;
-    TV_CUDA(cudaMemcpyAsync(m->tune_order.p, sample.data(), sizeof(int) * n_s, cudaMemcpyHostToDevice, st));
+  int64_t trial_len = 8LL * D;  // shorter (down to 2 D) when the batch holds fewer than 4 waves of them
+  if (total / trial_len < 4LL * m->sm_count) trial_len = std::max<int64_t>(2LL * D, total / (4LL * m->sm_count));
+  if (!tuned && tune_on && tune && n_seq >= 2 * m->sm_count && total / trial_len >= 2LL * m->sm_count) {
     struct Events {  // released on every return path
       cudaEvent_t a = nullptr, b = nullptr;
       ~Events() {
@@ -429,14 +428,22 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
     TV_CUDA(cudaEventCreate(&ev.a));
     TV_CUDA(cudaEventCreate(&ev.b));
     cudaEvent_t e0 = ev.a, e1 = ev.b;
-    float best_ms = 0.0f;
+    const int max_trials = (int)std::min<int64_t>(n_seq, total / trial_len);
+    if ((rc = m->tune_off.ensure((size_t)max_trials + 1)) != TV_OK) return rc;
+    std::vector<int64_t> toff((size_t)max_trials + 1);
+    for (int k = 0; k <= max_trials; ++k) toff[k] = (int64_t)k * trial_len;
+    // pageable source: the copy is staged before the call returns
+    TV_CUDA(cudaMemcpyAsync(m->tune_off.p, toff.data(), sizeof(int64_t) * toff.size(), cudaMemcpyHostToDevice,
+                            st));
+    double best_rate = 0.0;
     int best = kThreads;
     for (int shape : kCtaShapes) {
       int grid = 1;
-      if ((rc = prepare(shape, n_s, grid)) != TV_OK) break;
+      if ((rc = prepare(shape, max_trials, grid)) != TV_OK) break;
       tv::BatchView sv = bv;
-      sv.order = m->tune_order.p;
-      sv.n_seq = n_s;
+      sv.off = m->tune_off.p;
+      sv.order = nullptr;
+      sv.n_seq = grid;  // one full wave
       TV_CUDA(cudaMemsetAsync(m->counter.p, 0, sizeof(int), st));
       TV_CUDA(cudaEventRecord(e0, st));
       cta_kernel_for(shape)<<<grid, shape, dyn, st>>>(view(m, Q), sv, L, L.in_smem ? nullptr : m->scratch.p);
@@ -446,8 +453,9 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
       float ms = 0.0f;
       TV_CUDA(cudaEventElapsedTime(&ms, e0, e1));
       m->last_launches += 1;
-      if (shape == kCtaShapes[0] || ms < best_ms) {
-        best_ms = ms;
+      const double rate = (double)grid * (double)trial_len / std::max(1e-6, (double)ms);
+      if (rate > best_rate) {
+        best_rate = rate;
         best = shape;
       }
     }
@@ -460,6 +468,7 @@ int launch_batch(tv_model_s* m, int n_seq, const int64_t* off_host, const int32_
   int grid = 1;
   if ((rc = prepare(threads, n_seq, grid)) != TV_OK) return rc;
   m->batch_threads = threads;
+  m->batch_grid = grid;
   mark_start(m, st);
   cta_kernel_for(threads)<<<grid, threads, dyn, st>>>(view(m, Q), bv, L, L.in_smem ? nullptr : m->scratch.p);
   TV_CUDA(cudaGetLastError());
@@ -1276,6 +1285,8 @@ int tv_model_set_path(tv_model m, int path, int grid_ctas) {
 int tv_model_last_path(tv_model m) { return m ? m->last_path : 0; }
 
 int tv_model_batch_threads(tv_model m) { return m ? m->batch_threads : 0; }
+
+int tv_model_batch_grid(tv_model m) { return m ? m->batch_grid : 0; }
 
 int tv_model_drop_partial(tv_model m, int64_t step, int segment) {
   if (!m || step < 1 || step > 0xffffffffLL || segment < 0) return fail(TV_EINVAL, "bad argument");

@@ -50,6 +50,7 @@ EXPORTS = {
     "tv_model_set_path": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "tv_model_last_path": (C.c_int, [C.c_void_p]),
     "tv_model_batch_threads": (C.c_int, [C.c_void_p]),
+    "tv_model_batch_grid": (C.c_int, [C.c_void_p]),
     "tv_model_drop_partial": (C.c_int, [C.c_void_p, C.c_int64, C.c_int]),
     "tv_grid_plan_info": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     "tv_model_set_timing": (C.c_int, [C.c_void_p, C.c_int]),

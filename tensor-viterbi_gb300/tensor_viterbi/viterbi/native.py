@@ -207,6 +207,10 @@ class Model:
         shape), 0 before any."""
         return int(_lib.lib().tv_model_batch_threads(self._h))
 
+    def batch_grid(self) -> int:
+        """CTAs of the most recent batched decode, 0 before any."""
+        return int(_lib.lib().tv_model_batch_grid(self._h))
+
 
 class GaussianModel(Model):
     """A model whose emissions are Gaussian per state: the (T x N)
