@@ -44,6 +44,11 @@ struct FbArgs {
   int rings_in_smem;
   double* R;          // (J, tau) scratch of fb_small_kernel: r = pdf / N
   double* A;          // (J, tau) scratch of fb_small_kernel: sum_{i != j} p[i][j] F[i][t]
+  double* Q;          // (J, tau) scratch of fb_small_kernel<K > 0>: L1 / F (the backward
+                      // window's new entry), for the eta kernels
+  double* part;       // (J, nchunks, M) scratch: eta sums of the chunks of t
+  long long chunk;    // steps of t per chunk
+  int nchunks;
   int* status;        // 0, or 1 where the reference throws var_nonpositive_exception
 };
 
@@ -436,7 +441,9 @@ __global__ void __launch_bounds__(MAXT) fb_small_kernel(FbArgs a) {
       A_nx = at(a.A, jw, t - 1);
     }
     if (jw < J) {
-      s_tail = s_tail * r;  // the reference's s: r[tau-1] * r[tau-2] * ... * r[t+1]
+      // the reference's s: r[tau-1] * r[tau-2] * ... * r[t+1], read only
+      // while span <= M (the tail term and the right-censored eta terms)
+      if (span <= M) s_tail = s_tail * r;
       const double q = s_q[jw];  // L1(t+1) / F(t+1)
       double part = 0.0;
       if constexpr (K > 0) {
@@ -452,8 +459,7 @@ __global__ void __launch_bounds__(MAXT) fb_small_kernel(FbArgs a) {
             vk[k] = prev * r;
             const int u = lane + 1 + 32 * k;
             if (u < span && u <= M) {
-              part = __fma_rn(vk[k], dk[k], part);
-              ek[k] = __fma_rn(A, vk[k], ek[k]);
+              part = __fma_rn(vk[k], dk[k], part);  // its eta term A * V: fb_eta_chunk_kernel
             } else if (u == span) {
               part = __fma_rn(s_tail, DD(jw, span), part);
             }
@@ -506,29 +512,31 @@ __global__ void __launch_bounds__(MAXT) fb_small_kernel(FbArgs a) {
         at(a.L, gj, t) = lv;
         Lnext = lv;
         s_q[gj] = sv;
+        if (K > 0) at(a.Q, gj, t) = sv;
       }
     }
     __syncthreads();
   }
 
+  // K > 0: eta's right-censored terms (A * s) go to eta; fb_eta_chunk_kernel
+  // and fb_eta_final_kernel add the window terms and finish it.
+  if constexpr (K > 0) {
+    if (jw < J) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const int u = lane + 1 + 32 * k;
+        if (u <= M) a.eta[(size_t)jw * M + (u - 1)] = ek[k];
+      }
+    }
+    if (tid == 0) *a.status = 0;
+    return;
+  }
   // eta = d(u) * (accumulated A * V and A * s) + the segment that starts at
   // t = 0 (FBImpl.cpp:252-266)
   if (jw < J) {
     const int j = jw;
-    for (int k = 0, u = lane + 1; u <= M; ++k, u += 32) {
-      double w;
-      if constexpr (K > 0) {
-        double e = 0.0, dv = 0.0;
-#pragma unroll
-        for (int m = 0; m < K; ++m)
-          if (m == k) {
-            e = ek[m];
-            dv = dk[m];
-          }
-        w = e * dv;
-      } else {
-        w = Et[(size_t)j * M + (u - 1)] * dd(j, u);
-      }
+    for (int u = lane + 1; u <= M; u += 32) {
+      double w = Et[(size_t)j * M + (u - 1)] * dd(j, u);
       if (right || u <= tau - 1) {
         double r = dd(j, u) * a.pi[j];
         if (u <= tau - 1) {
@@ -543,6 +551,94 @@ __global__ void __launch_bounds__(MAXT) fb_small_kernel(FbArgs a) {
     }
   }
   if (tid == 0) *a.status = 0;
+}
+
+// The eta term of the segment that starts at t = 0 (FBImpl.cpp:252-266).
+__device__ __forceinline__ double fb_eta_initial(const FbArgs& a, int j, int u) {
+  const int tau = a.tau, M = a.M;
+  double r = __ldg(a.d + (size_t)j * M + (u - 1)) * a.pi[j];
+  if (u <= tau - 1) {
+    for (int v = 1; v <= u; ++v) r *= a.pdf[(size_t)j * tau + (u - v)] / a.N[u - v];
+    r *= a.L1[(size_t)j * tau + (u - 1)] / a.F[(size_t)j * tau + (u - 1)];
+  } else {
+    for (int v = 1; v <= tau; ++v) r *= a.pdf[(size_t)j * tau + (tau - v)] / a.N[tau - v];
+  }
+  return r;
+}
+
+// fb_eta_chunk_kernel: the window terms of eta, off the backward chain.
+// eta[j][u] collects A[j][t] * V_t(u) over the steps t with t + u <= tau - 2,
+// where V_t(u) = r[t+1] * V_{t+1}(u-1) and V_t(1) = r[t+1] * Q[t+1] is the
+// backward window of fb_small_kernel (the same products in the same order,
+// from the ratios R and the entries Q it stored).  One warp per (chunk of t,
+// state): it rebuilds the window from M - 1 steps above its chunk (an entry
+// for segment end e enters at t = e - 1), then accumulates over the chunk,
+// the window in registers moved by shuffles as in the backward pass.
+template <int K>
+__global__ void __launch_bounds__(32) fb_eta_chunk_kernel(FbArgs a) {
+  if (*a.status != 0) return;
+  const int j = blockIdx.y, c = blockIdx.x, lane = threadIdx.x;
+  const int tau = a.tau, M = a.M;
+  const long long t0 = (long long)c * a.chunk;
+  const long long t1 = min((long long)tau - 1, t0 + a.chunk);  // t in [t0, t1), t <= tau - 2
+  double vk[K], acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) vk[k] = acc[k] = 0.0;
+  const double* R = a.R + (size_t)j * tau;
+  const double* Qr = a.Q + (size_t)j * tau;
+  const double* Ar = a.A + (size_t)j * tau;
+  const long long ts = min((long long)tau - 2, t1 + M - 2);
+  // a step's ratio, entry and weight, loaded a step ahead
+  double r_nx = 0.0, q_nx = 0.0, A_nx = 0.0;
+  if (ts >= t0) {
+    r_nx = R[ts + 1];
+    q_nx = ts + 1 <= tau - 2 ? Qr[ts + 1] : 0.0;
+    A_nx = Ar[ts];
+  }
+  for (long long t = ts; t >= t0; --t) {
+    const double r = r_nx, q = q_nx, A = A_nx;
+    if (t - 1 >= t0) {
+      r_nx = R[t];
+      q_nx = t <= tau - 2 ? Qr[t] : 0.0;
+      A_nx = Ar[t - 1];
+    }
+    double carry = 0.0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const double up = __shfl_up_sync(0xffffffffu, vk[k], 1);
+      const double top = __shfl_sync(0xffffffffu, vk[k], 31);
+      const double prev = lane == 0 ? (k == 0 ? q : carry) : up;
+      carry = top;
+      vk[k] = prev * r;
+    }
+    if (t < t1) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const int u = lane + 1 + 32 * k;
+        if (u <= M && t + u <= tau - 2) acc[k] = __fma_rn(A, vk[k], acc[k]);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int u = lane + 1 + 32 * k;
+    if (u <= M) a.part[((size_t)j * a.nchunks + c) * M + (u - 1)] = acc[k];
+  }
+}
+
+// fb_eta_final_kernel: eta = d(u) * (right-censored terms + the chunks' window
+// terms, chunks in order) + the term of the segment that starts at t = 0.
+__global__ void fb_eta_final_kernel(FbArgs a) {
+  if (*a.status != 0) return;
+  const int j = blockIdx.x, M = a.M;
+  const bool right = a.censoring == 1;
+  for (int u = threadIdx.x + 1; u <= M; u += blockDim.x) {
+    double w = 0.0;
+    for (int c = 0; c < a.nchunks; ++c) w += a.part[((size_t)j * a.nchunks + c) * M + (u - 1)];
+    w = (a.eta[(size_t)j * M + (u - 1)] + w) * __ldg(a.d + (size_t)j * M + (u - 1));
+    if (right || u <= a.tau - 1) w += fb_eta_initial(a, j, u);
+    a.eta[(size_t)j * M + (u - 1)] = w;
+  }
 }
 
 }  // namespace tv

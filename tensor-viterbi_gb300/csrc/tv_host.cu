@@ -965,8 +965,21 @@ int fb_run(int censoring, int64_t tau, int J, int M, const double* d, const doub
   const size_t ring_bytes = nrings * JM * sizeof(double);
   const bool in_smem = ring_bytes + 2048 <= (size_t)smem_optin;
   if (!in_smem && b.get(&dring, nrings * JM)) return fail(TV_ENOMEM, "tv_fb: device allocation failed");
-  double *dR = nullptr, *dA = nullptr;
+  double *dR = nullptr, *dA = nullptr, *dQ = nullptr, *dpart = nullptr;
   if (small && (b.get(&dR, JT) || b.get(&dA, JT))) return fail(TV_ENOMEM, "tv_fb: device allocation failed");
+  // register path: eta's window terms in chunks of t over the whole GPU
+  // (about eight warps per SM, chunks of at least 4 M steps)
+  long long chunk = 1;
+  int nchunks = 1;
+  if (regs) {
+    int sms = 1;
+    TV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const long long steps = std::max<long long>(1, (long long)tau - 1);
+    chunk = std::max<long long>(4LL * M, (steps * J + 8LL * sms - 1) / (8LL * sms));
+    nchunks = (int)((steps + chunk - 1) / chunk);
+    if (b.get(&dQ, JT) || b.get(&dpart, (size_t)J * nchunks * M))
+      return fail(TV_ENOMEM, "tv_fb: device allocation failed");
+  }
   TV_CUDA(cudaMemcpy(dd, d, sizeof(double) * JM, cudaMemcpyHostToDevice));
   TV_CUDA(cudaMemcpy(dp, p, sizeof(double) * J * J, cudaMemcpyHostToDevice));
   TV_CUDA(cudaMemcpy(dpi, pi, sizeof(double) * J, cudaMemcpyHostToDevice));
@@ -981,7 +994,7 @@ int fb_run(int censoring, int64_t tau, int J, int M, const double* d, const doub
   A.d = dd; A.p = dp; A.pi = dpi; A.pdf = dpdf;
   A.F = dF; A.L = dL; A.G = dG; A.L1 = dL1; A.N = dN; A.Norm = dNorm; A.eta = deta;
   A.S = dS; A.D = dD; A.ring = dring; A.rings_in_smem = in_smem ? 1 : 0; A.status = dst;
-  A.R = dR; A.A = dA;
+  A.R = dR; A.A = dA; A.Q = dQ; A.part = dpart; A.chunk = chunk; A.nchunks = nchunks;
   const int threads = 32 * std::min(32, J);
   const size_t dyn = in_smem ? ring_bytes : 0;
   constexpr int KR = tv::FB_REG_BLOCKS;
@@ -999,6 +1012,12 @@ int fb_run(int censoring, int64_t tau, int J, int M, const double* d, const doub
   else if (!regs) tv::fb_small_kernel<0, 1024><<<1, threads, dyn>>>(A);
   else if (J <= 16) tv::fb_small_kernel<KR, 512><<<1, threads, dyn>>>(A);
   else tv::fb_small_kernel<KR, 1024><<<1, threads, dyn>>>(A);
+  if (regs) {
+    TV_CUDA(cudaGetLastError());
+    tv::fb_eta_chunk_kernel<KR><<<dim3(nchunks, J), 32>>>(A);
+    TV_CUDA(cudaGetLastError());
+    tv::fb_eta_final_kernel<<<J, 128>>>(A);
+  }
   TV_CUDA(cudaGetLastError());
   TV_CUDA(cudaEventRecord(b.e1));
   TV_CUDA(cudaEventSynchronize(b.e1));
