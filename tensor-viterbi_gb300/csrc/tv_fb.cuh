@@ -391,15 +391,27 @@ __global__ void __launch_bounds__(MAXT) fb_small_kernel(FbArgs a) {
     if (s_bad) break;
     if (t < tau - 1 && warp * per_warp < J) {
       const double pr = (gj < J && gi < J) ? pp(gi, gj) * s_F[gi] : 0.0;
-      double sv = pr, av = gi != gj ? pr : 0.0;
-      for (int o = Gs >> 1; o > 0; o >>= 1) {
-        sv += __shfl_xor_sync(0xffffffffu, sv, o);
-        av += __shfl_xor_sync(0xffffffffu, av, o);
-      }
-      if (glead) {
-        s_S[gj] = sv;
-        at(a.S, gj, t + 1) = sv;
-        at(a.A, gj, t) = av;
+      // the eta weight A[t] is read by the backward pass only while
+      // tau - 1 - t <= M with K > 0 (fb_eta_chunk_kernel forms the rest
+      // itself, in the same order), at every step with K = 0
+      if (K == 0 || t >= tau - 1 - M) {
+        double sv = pr, av = gi != gj ? pr : 0.0;
+        for (int o = Gs >> 1; o > 0; o >>= 1) {
+          sv += __shfl_xor_sync(0xffffffffu, sv, o);
+          av += __shfl_xor_sync(0xffffffffu, av, o);
+        }
+        if (glead) {
+          s_S[gj] = sv;
+          at(a.S, gj, t + 1) = sv;
+          at(a.A, gj, t) = av;
+        }
+      } else {
+        double sv = pr;
+        for (int o = Gs >> 1; o > 0; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o);
+        if (glead) {
+          s_S[gj] = sv;
+          at(a.S, gj, t + 1) = sv;
+        }
       }
     }
     __syncthreads();
@@ -584,23 +596,29 @@ __global__ void __launch_bounds__(32) fb_eta_chunk_kernel(FbArgs a) {
   double vk[K], acc[K];
 #pragma unroll
   for (int k = 0; k < K; ++k) vk[k] = acc[k] = 0.0;
+  const int J = a.J;
   const double* R = a.R + (size_t)j * tau;
   const double* Qr = a.Q + (size_t)j * tau;
-  const double* Ar = a.A + (size_t)j * tau;
+  // the eta weight A[t] = sum_{i != j} p[i][j] F[i][t], lane i the term of
+  // state i: the same products and the same xor tree as the forward pass's
+  // lane groups (lanes past the group add zeros), so the same values
+  const bool has_i = lane < J && lane != j;
+  const double pij = has_i ? __ldg(a.p + (size_t)lane * J + j) : 0.0;
+  const double* Fi = a.F + (size_t)(lane < J ? lane : 0) * tau;
   const long long ts = min((long long)tau - 2, t1 + M - 2);
-  // a step's ratio, entry and weight, loaded a step ahead
-  double r_nx = 0.0, q_nx = 0.0, A_nx = 0.0;
+  // a step's ratio, entry and F term, loaded a step ahead
+  double r_nx = 0.0, q_nx = 0.0, f_nx = 0.0;
   if (ts >= t0) {
     r_nx = R[ts + 1];
     q_nx = ts + 1 <= tau - 2 ? Qr[ts + 1] : 0.0;
-    A_nx = Ar[ts];
+    f_nx = has_i ? Fi[ts] : 0.0;
   }
   for (long long t = ts; t >= t0; --t) {
-    const double r = r_nx, q = q_nx, A = A_nx;
+    const double r = r_nx, q = q_nx, f = f_nx;
     if (t - 1 >= t0) {
       r_nx = R[t];
       q_nx = t <= tau - 2 ? Qr[t] : 0.0;
-      A_nx = Ar[t - 1];
+      f_nx = has_i ? Fi[t - 1] : 0.0;
     }
     double carry = 0.0;
 #pragma unroll
@@ -612,6 +630,7 @@ __global__ void __launch_bounds__(32) fb_eta_chunk_kernel(FbArgs a) {
       vk[k] = prev * r;
     }
     if (t < t1) {
+      const double A = warp_sum(has_i ? pij * f : 0.0);
 #pragma unroll
       for (int k = 0; k < K; ++k) {
         const int u = lane + 1 + 32 * k;
