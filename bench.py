@@ -643,7 +643,7 @@ def run_served(args, w, wname):
             for item in pool.imap(make, range(n), chunksize=2):
                 made.put(item)
 
-        with native.Server() as srv:
+        with native.Server(max_inflight=args.max_inflight) as srv:
             prod = threading.Thread(target=producer, daemon=True)
             prod.start()
             ready = [made.get() for _ in range(n)] if rate is None else []  # a burst: all made first
@@ -690,7 +690,7 @@ def run_served(args, w, wname):
     cap = run_rate(n_cap, None)
     capacity = cap["requests_per_s"]
     out = []
-    loads = [float(x) for x in args.loads.split(",")] if args.loads else w["loads"]
+    loads = ([] if args.loads == "none" else [float(x) for x in args.loads.split(",")]) if args.loads else w["loads"]
     for f in loads:
         r = run_rate(n_req, f * capacity)
         r.update({"offered_load": f, "rate_per_s": f * capacity})
@@ -895,7 +895,9 @@ def main():
     ap.add_argument("--T", type=int, default=0, help="override the sequence length (profiling runs)")
     ap.add_argument("--n-seq", type=int, default=0, help="batched workload: override the number of sequences "
                                                          "(profiling runs)")
-    ap.add_argument("--loads", default="", help="served workload: comma-separated fractions of the capacity")
+    ap.add_argument("--loads", default="", help="served workload: comma-separated fractions of the capacity "
+                                                "('none': capacity only)")
+    ap.add_argument("--max-inflight", type=int, default=64, help="served workload: requests in flight at most")
     ap.add_argument("--requests", type=int, default=0, help="served workload: number of requests per rate")
     ap.add_argument("--capacity-requests", type=int, default=1000,
                     help="served workload: requests in the burst that measures the capacity")
