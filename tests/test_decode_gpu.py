@@ -101,6 +101,31 @@ def test_batch_autotuned_cta_shape(tvlib):
         del os.environ["TV_AUTOTUNE"]
 
 
+def test_batch_with_the_duration_table_in_global_memory(tvlib, monkeypatch):
+    """A batch with more sequences than the full work area's grid holds (N=10,
+    D=250: two CTAs of 86 KB per SM) leaves the duration table in global
+    memory so that a third CTA shares each SM; every path equals the
+    one-at-a-time decode (a lone CTA keeps the full work area) and the oracle
+    on a sample."""
+    import torch
+    import tensor_viterbi.synthetic as syn
+    monkeypatch.setenv("TV_AUTOTUNE", "0")  # 256 threads: three CTAs fit an SM without the table
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    prob, seqs = syn.batch_problem(n_seq=3 * sms + 24, N=10, D=250, M=16, lo=260, hi=700, seed=31)
+    with tvlib.Model(*prob.model_args()) as m:
+        paths, lls = m.decode_batch(seqs, return_loglik=True)
+        assert m.batch_threads() == 256
+        assert m.batch_grid() == 3 * sms
+        for k in range(0, len(seqs), 41):
+            p1, l1 = m.decode(seqs[k], return_loglik=True)
+            np.testing.assert_array_equal(paths[k], p1)
+            assert lls[k] == l1
+            if k % 123 == 0:
+                ref = orc.decode(*prob.model_args(), seqs[k])
+                np.testing.assert_array_equal(p1, ref["path"])
+                assert l1 == ref["loglik"]
+
+
 def test_errors_are_returned_not_fatal(tvlib):
     args, _ = load_golden("syn_config0")
     N, tm, em, dl, sp, dp, obs = args
