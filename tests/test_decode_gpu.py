@@ -135,6 +135,11 @@ def test_errors_are_returned_not_fatal(tvlib):
     bad[3] = 99
     with pytest.raises(ValueError, match="outside"):
         tvlib.decode_tensor_viterbi_cuda(N, tm, em, dl, sp, dp, bad)
+    # in a batch the kernel's own range check reports the sequence
+    with tvlib.Model(N, tm, em, dl, sp, dp) as m:
+        with pytest.raises(ValueError, match="sequence 1 has an observation outside"):
+            m.decode_batch([obs, bad, obs])
+        np.testing.assert_array_equal(m.decode_batch([obs, obs])[1], orc.decode(*args)["path"])
     # the library stays usable after an error
     np.testing.assert_array_equal(tvlib.decode_tensor_viterbi_cuda(*args), orc.decode(*args)["path"])
 
