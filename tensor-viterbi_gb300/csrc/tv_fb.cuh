@@ -16,7 +16,8 @@
 // (forward) or last (backward) step, or in registers), and multiplied by the
 // new ratio every step (one multiply per cell, like the decoder's window
 // folds), instead of being rebuilt for every u as the reference does; and
-// the sums over u are lane partials reduced by shuffles.  Both change the
+// the sums over u are lane partials reduced by shuffles (or, for the window
+// sums of fb_small_kernel, exactly in 64-bit integers).  Both change the
 // association of some products and sums, so results agree with the
 // reference to rounding (relative differences of order 1e-13 on the tests'
 // sequences), not bit for bit.  The backward right-censoring product s is
@@ -261,15 +262,20 @@ constexpr int FB_REG_BLOCKS = 4;
 //             reduction in 64-bit integers (fixed_group_sum: ten warps of
 //             double-add trees would occupy the SM's FP64 unit);
 //             groups of lanes (a power of two >= J per state) form
-//             StateIn[j][t+1] and the eta weight A[j][t] = sum_{i != j} p[i][j] F[i][t].
+//             StateIn[j][t+1], and the eta weight A[j][t] = sum_{i != j}
+//             p[i][j] F[i][t] where the backward pass reads it (every step
+//             with K = 0; the last M steps with K > 0).
 //   backward: warp j keeps V(u) = Q(t+1..t+u) * L1(t+u) / F(t+u) for the
 //             segment that ends at t+u, V(u-1) of step t+1 times r, the same
-//             way, so a segment term is V(u) * d(u); the eta accumulators take
-//             A * V without the factor d(u), applied once at the end; the
-//             right-censoring product s is formed in the reference's order;
-//             groups of lanes form L1 = F * sum_k G[k] p[j][k] and L, and
-//             L1 / F is taken as that sum.
-// The ratios and weights of the forward pass are kept for the backward pass.
+//             way, so a segment term is V(u) * d(u); groups of lanes form
+//             L1 = F * sum_k G[k] p[j][k] and L, and L1 / F is taken as that
+//             sum.  Eta: with K = 0 the accumulators take A * V (and the
+//             right-censored terms A * s, s formed in the reference's order)
+//             without the factor d(u), applied once at the end; with K > 0
+//             only the right-censored terms are taken here, L1 / F is stored
+//             per step, and fb_eta_chunk_kernel / fb_eta_final_kernel form the
+//             A * V terms off this chain and finish eta.
+// The ratios of the forward pass are kept for the backward pass.
 // Products, the sums over u, i, k and j, fused multiply-adds and the
 // divisions associate differently from the reference (which sums in order
 // and divides each term), which moves results by rounding only.
